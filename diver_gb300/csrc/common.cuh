@@ -1,0 +1,137 @@
+// Shared device helpers for the DIVeR hot-path kernels (sm_103a).
+//
+// Every floating-point step of the voxel walk is written with explicit
+// round-to-nearest intrinsics (__fadd_rn, __fmul_rn, __fdiv_rn, __fmaf_rn) so
+// the result does not depend on the compiler's contraction choices.  The walk
+// reproduces the reference kernels' arithmetic exactly:
+//   utils/ray_voxel_intersection/src/ray_voxel_intersect.cu:53-150 (dense)
+//   utils/ray_voxel_intersection/src/ray_voxel_intersect.cu:216-318 (masked)
+//   utils/ray_march/src/ray_march.cu:58-145,184-227 (octree + march)
+// The reference is compiled with the default -fmad=true, which contracts the
+// position update `ori + dir*t` into one fused multiply-add; the products
+// `ori*step` and `floor(..)*step` are exact (step is -1, 0 or +1), so writing
+// them fused or unfused gives the same bits.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/diver_gb300.h"
+
+namespace dv {
+
+// Sign of x as -1, 0 or +1 (reference ray_voxel_intersect.cu:9-13).
+__device__ __forceinline__ float step_sign(float x) {
+  return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);
+}
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) {
+  return fmaxf(lo, fminf(v, hi));
+}
+
+// Slab test of the ray (p, d) against the box [0, n]^3 in voxel units.
+// When p lies inside the box it is kept and t = 0.  Otherwise p becomes the
+// clamped point p + d*tmin and t = tmin.  Returns false on a miss (tmin > tmax);
+// p still holds the clamped point then, which the dense walk records.
+// Reference: ray_voxel_intersect.cu:61-100, ray_march.cu:58-88.
+__device__ __forceinline__ bool box_entry(float3& p, const float3 d, const float n, float& t) {
+  const bool inside = (p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) &
+                      (p.x <= n) & (p.y <= n) & (p.z <= n);
+  if (inside) {
+    t = 0.f;
+    return true;
+  }
+  float a = __fdiv_rn(-p.x, d.x), b = __fdiv_rn(__fsub_rn(n, p.x), d.x);
+  float lo = fminf(a, b), hi = fmaxf(a, b);
+  a = __fdiv_rn(-p.y, d.y);
+  b = __fdiv_rn(__fsub_rn(n, p.y), d.y);
+  lo = fmaxf(lo, fminf(a, b));
+  hi = fminf(hi, fmaxf(a, b));
+  a = __fdiv_rn(-p.z, d.z);
+  b = __fdiv_rn(__fsub_rn(n, p.z), d.z);
+  lo = fmaxf(lo, fminf(a, b));
+  hi = fminf(hi, fmaxf(a, b));
+  p.x = clampf(__fmaf_rn(d.x, lo, p.x), 0.f, n);
+  p.y = clampf(__fmaf_rn(d.y, lo, p.y), 0.f, n);
+  p.z = clampf(__fmaf_rn(d.z, lo, p.z), 0.f, n);
+  t = lo;
+  return !(lo > hi);
+}
+
+// One step of the 3D-DDA: from point a, move along d to the nearest grid
+// plane crossing b; dt is the parameter increment.  The coordinate of the
+// plane that was hit is snapped onto the plane, with ties resolved x, then y,
+// then z.  Reference: ray_voxel_intersect.cu:119-135.
+__device__ __forceinline__ void grid_step(const float3 a, const float3 d, const float3 s,
+                                          float3& b, float& dt) {
+  const float bx = __fmul_rn(floorf(__fmaf_rn(a.x, s.x, 1.f)), s.x);
+  const float by = __fmul_rn(floorf(__fmaf_rn(a.y, s.y, 1.f)), s.y);
+  const float bz = __fmul_rn(floorf(__fmaf_rn(a.z, s.z, 1.f)), s.z);
+  const float tx = __fdiv_rn(__fsub_rn(bx, a.x), d.x);
+  const float ty = __fdiv_rn(__fsub_rn(by, a.y), d.y);
+  const float tz = __fdiv_rn(__fsub_rn(bz, a.z), d.z);
+  dt = fminf(tx, fminf(ty, tz));
+  b.x = __fmaf_rn(d.x, dt, a.x);
+  b.y = __fmaf_rn(d.y, dt, a.y);
+  b.z = __fmaf_rn(d.z, dt, a.z);
+  if (dt == tx) {
+    b.x = bx;
+  } else if (dt == ty) {
+    b.y = by;
+  } else {
+    b.z = bz;
+  }
+}
+
+// True when b has left [0, n]^3 (dense and masked walks: a point on the far
+// face is still inside).  Reference: ray_voxel_intersect.cu:137-138.
+__device__ __forceinline__ bool outside_closed(const float3 b, const float n) {
+  return (b.x < 0.f) | (b.y < 0.f) | (b.z < 0.f) | (b.x > n) | (b.y > n) | (b.z > n);
+}
+
+// True when b has left [0, n)^3 (real-time march).  Reference: ray_march.cu:203-204.
+__device__ __forceinline__ bool outside_open(const float3 b, const float n) {
+  return (b.x < 0.f) | (b.y < 0.f) | (b.z < 0.f) | (b.x >= n) | (b.y >= n) | (b.z >= n);
+}
+
+// Linear index of the occupancy cell that holds the voxel between a and b,
+// on a grid of m cells per side scaled by `scale` from voxel units.
+// Reference: ray_voxel_intersect.cu:297-299, ray_march.cu:132-135,211-212.
+__device__ __forceinline__ long long cell_index(const float3 a, const float3 b, float scale, int m) {
+  const float cx = __fmul_rn(fminf(__fadd_rn(a.x, 1e-4f), __fadd_rn(b.x, 1e-4f)), scale);
+  const float cy = __fmul_rn(fminf(__fadd_rn(a.y, 1e-4f), __fadd_rn(b.y, 1e-4f)), scale);
+  const float cz = __fmul_rn(fminf(__fadd_rn(a.z, 1e-4f), __fadd_rn(b.z, 1e-4f)), scale);
+  return (long long)(int)cz * m * m + (long long)(int)cy * m + (int)cx;
+}
+
+// Same index without the scale factor (scale == 1 multiplies exactly).
+__device__ __forceinline__ long long cell_index1(const float3 a, const float3 b, int m) {
+  const float cx = fminf(__fadd_rn(a.x, 1e-4f), __fadd_rn(b.x, 1e-4f));
+  const float cy = fminf(__fadd_rn(a.y, 1e-4f), __fadd_rn(b.y, 1e-4f));
+  const float cz = fminf(__fadd_rn(a.z, 1e-4f), __fadd_rn(b.z, 1e-4f));
+  return (long long)(int)cz * m * m + (long long)(int)cy * m + (int)cx;
+}
+
+// Reads one occupancy byte; an index outside the mask (a degenerate walk
+// along the far face) counts as empty instead of reading past the buffer.
+__device__ __forceinline__ bool occupied(const uint8_t* __restrict__ mask, long long idx, long long cells) {
+  return (idx >= 0 && idx < cells) ? (__ldg(mask + idx) != 0) : false;
+}
+
+__host__ __device__ __forceinline__ unsigned ceil_div(long long a, long long b) {
+  return (unsigned)((a + b - 1) / b);
+}
+
+}  // namespace dv
+
+// Error helpers used by every C-ABI entry point: a launch failure becomes a
+// status code, never a process exit.
+#define DV_TRY_LAUNCH()                                   \
+  do {                                                    \
+    cudaError_t e__ = cudaGetLastError();                 \
+    if (e__ != cudaSuccess) return DV_ERR_CUDA;           \
+  } while (0)
+
+#define DV_CHECK(cond, code) \
+  do {                       \
+    if (!(cond)) return (code); \
+  } while (0)

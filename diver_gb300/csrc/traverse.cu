@@ -1,0 +1,553 @@
+// Voxel traversal kernels: dense and masked 3D-DDA (training/offline path),
+// the octree first-hit search and the 8-hit ray march (real-time path), and
+// the prefix sum that turns per-ray counts into CSR segment offsets.
+//
+// One thread walks one ray; the walk itself is inherently sequential (each
+// crossing is computed from the previous, rounded point), so bit-exactness
+// with the reference fixes the per-ray order of operations.  What changes
+// against the reference is around the walk: outputs are either counted only,
+// written to caller-sized padded rows, or written compacted (CSR) so that the
+// segment-parallel decoder never touches padding; max(count) is reduced per
+// warp before one atomic; launches are stream-ordered with no device sync.
+#include "common.cuh"
+
+namespace dv {
+
+enum WalkMode { WALK_COUNT = 0, WALK_PADDED = 1, WALK_SEGMENTS = 2 };
+
+struct WalkArgs {
+  int batch;
+  int max_n;
+  float xyzmin;
+  float n;
+  float voxel_size;
+  float mask_scale;
+  int m;            // occupancy cells per side
+  long long cells;  // m^3
+  const float* o;
+  const float* v;
+  const uint8_t* mask;
+  float* inter;
+  int* num;
+  float* tns;
+  int* max_count;
+  const int64_t* offsets;
+  float* seg;
+  float* seg_t;
+  int* seg_ray;
+};
+
+__device__ __forceinline__ void warp_max_atomic(int* dst, int value, bool active) {
+  const unsigned full = __activemask();
+  const int mx = __reduce_max_sync(full, active ? value : 0);
+  if (dst != nullptr && (threadIdx.x & 31) == (__ffs(full) - 1)) atomicMax(dst, mx);
+}
+
+__device__ __forceinline__ float3 ray_origin_voxel(const float* o, int b, float xyzmin, float vs) {
+  return make_float3(__fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 0), xyzmin), vs),
+                     __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 1), xyzmin), vs),
+                     __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 2), xyzmin), vs));
+}
+
+__device__ __forceinline__ float3 load3(const float* p, int b) {
+  return make_float3(__ldg(p + 3 * b + 0), __ldg(p + 3 * b + 1), __ldg(p + 3 * b + 2));
+}
+
+__device__ __forceinline__ float3 signs(float3 d) {
+  return make_float3(step_sign(d.x), step_sign(d.y), step_sign(d.z));
+}
+
+// Dense walk: entry point, then every plane crossing while the point stays
+// in [0,n]^3.  Reference ray_voxel_intersect.cu:39-150.
+template <int MODE>
+__global__ void __launch_bounds__(256) dense_walk_kernel(const WalkArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = b < a.batch;
+  int count = 0;
+  if (live) {
+    const float3 d = load3(a.v, b);
+    float3 p = ray_origin_voxel(a.o, b, a.xyzmin, a.voxel_size);
+    float t;
+    const bool hit = box_entry(p, d, a.n, t);
+    float* row = nullptr;
+    float* trow = nullptr;
+    int64_t base = 0, cap = 0;
+    if (MODE == WALK_PADDED) {
+      row = a.inter + (long long)b * a.max_n * 3;
+      trow = a.tns + (long long)b * a.max_n;
+      if (a.max_n > 0) {
+        row[0] = p.x;
+        row[1] = p.y;
+        row[2] = p.z;
+      }
+    }
+    if (MODE == WALK_SEGMENTS) {
+      base = a.offsets[b];
+      cap = a.offsets[b + 1] - base;
+    }
+    if (hit) {
+      if (MODE == WALK_PADDED && a.max_n > 0) trow[0] = __fmul_rn(t, a.voxel_size);
+      count = 1;
+      const float3 s = signs(d);
+      float3 q;
+      float dt;
+      while (true) {
+        grid_step(p, d, s, q, dt);
+        const float tq = __fadd_rn(t, dt);
+        if (outside_closed(q, a.n)) break;
+        if (MODE == WALK_PADDED && count < a.max_n) {
+          row[3 * count + 0] = q.x;
+          row[3 * count + 1] = q.y;
+          row[3 * count + 2] = q.z;
+          trow[count] = __fmul_rn(tq, a.voxel_size);
+        }
+        if (MODE == WALK_SEGMENTS && count - 1 < cap) {
+          float* sg = a.seg + (base + count - 1) * 6;
+          sg[0] = p.x;
+          sg[1] = p.y;
+          sg[2] = p.z;
+          sg[3] = q.x;
+          sg[4] = q.y;
+          sg[5] = q.z;
+          if (a.seg_t) a.seg_t[base + count - 1] = __fmul_rn(t, a.voxel_size);
+          if (a.seg_ray) a.seg_ray[base + count - 1] = b;
+        }
+        ++count;
+        p = q;
+        t = tq;
+      }
+    }
+    if (MODE != WALK_SEGMENTS) a.num[b] = count;
+  }
+  if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
+}
+
+// Masked walk: (entry, exit) of every voxel whose occupancy byte is set.
+// Reference ray_voxel_intersect.cu:203-318.
+template <int MODE>
+__global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = b < a.batch;
+  int count = 0;
+  if (live) {
+    const float3 d = load3(a.v, b);
+    float3 p = ray_origin_voxel(a.o, b, a.xyzmin, a.voxel_size);
+    float t;
+    if (box_entry(p, d, a.n, t)) {
+      const float3 s = signs(d);
+      float* row = nullptr;
+      float* trow = nullptr;
+      int64_t base = 0, cap = 0;
+      if (MODE == WALK_PADDED) {
+        row = a.inter + (long long)b * a.max_n * 6;
+        trow = a.tns + (long long)b * a.max_n;
+      }
+      if (MODE == WALK_SEGMENTS) {
+        base = a.offsets[b];
+        cap = a.offsets[b + 1] - base;
+      }
+      float3 q;
+      float dt;
+      while (true) {
+        grid_step(p, d, s, q, dt);
+        t = __fadd_rn(t, dt);
+        if (outside_closed(q, a.n)) break;
+        const long long idx = cell_index(p, q, a.mask_scale, a.m);
+        if (occupied(a.mask, idx, a.cells)) {
+          if (MODE == WALK_PADDED && count < a.max_n) {
+            float* r = row + 6 * count;
+            r[0] = p.x;
+            r[1] = p.y;
+            r[2] = p.z;
+            r[3] = q.x;
+            r[4] = q.y;
+            r[5] = q.z;
+            trow[count] = __fmul_rn(t, a.voxel_size);
+          }
+          if (MODE == WALK_SEGMENTS && count < cap) {
+            float* sg = a.seg + (base + count) * 6;
+            sg[0] = p.x;
+            sg[1] = p.y;
+            sg[2] = p.z;
+            sg[3] = q.x;
+            sg[4] = q.y;
+            sg[5] = q.z;
+            if (a.seg_t) a.seg_t[base + count] = __fmul_rn(t, a.voxel_size);
+            if (a.seg_ray) a.seg_ray[base + count] = b;
+          }
+          ++count;
+        }
+        p = q;
+      }
+    }
+    if (MODE != WALK_SEGMENTS) a.num[b] = count;
+  }
+  if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
+}
+
+// Octree first hit.  Reference ray_march.cu:33-148, generalised from the
+// N in {128, 256} templates to any N that is a multiple of 64.
+__global__ void __launch_bounds__(256) aabb_kernel(int batch, float* __restrict__ coords,
+                                                   const float* __restrict__ v,
+                                                   const float* __restrict__ center,
+                                                   uint8_t* __restrict__ finish,
+                                                   float* __restrict__ rgba,
+                                                   const uint8_t* __restrict__ oct, int N,
+                                                   long long oct_cells) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  float* slot = coords + (long long)batch * 6 * 7 + (long long)b * 6 + 3;
+  reinterpret_cast<float4*>(rgba)[b] = make_float4(0.f, 0.f, 0.f, 1.f);
+  finish[b] = 0;
+  const float3 d = load3(v, b);
+  float3 p = make_float3(__ldg(center + 0), __ldg(center + 1), __ldg(center + 2));
+  float t;
+  if (!box_entry(p, d, (float)N, t)) {
+    slot[0] = -1.f;
+    finish[b] = 1;
+    return;
+  }
+  p = make_float3(__fmul_rn(p.x, 0.015625f), __fmul_rn(p.y, 0.015625f), __fmul_rn(p.z, 0.015625f));
+  const float3 s = signs(d);
+  int m = N / 64;
+  long long off = 0;
+  float3 last = p;
+  while (m < N) {
+    last = p;
+    float3 q;
+    float dt;
+    grid_step(last, d, s, q, dt);
+    if (outside_closed(q, (float)m)) {
+      slot[0] = -1.f;
+      finish[b] = 1;
+      return;
+    }
+    const long long idx = off + cell_index1(last, q, m);
+    if (occupied(oct, idx, oct_cells)) {
+      off += (long long)m * m * m;
+      last = make_float3(__fmul_rn(last.x, 4.f), __fmul_rn(last.y, 4.f), __fmul_rn(last.z, 4.f));
+      p = last;
+      m *= 4;
+    } else {
+      p = q;
+    }
+  }
+  slot[0] = last.x;
+  slot[1] = last.y;
+  slot[2] = last.z;
+}
+
+// Next 8 occupied voxels.  Reference ray_march.cu:159-229.  The reference
+// leaves its grid-stride loop when an unfinished ray has no resume point
+// (x < 0), a state that aabb_intersect + mlp_eval never produce; here such a
+// ray is skipped on its own so the result does not depend on the launch shape.
+__global__ void __launch_bounds__(256) march_kernel(int batch, float* __restrict__ coords,
+                                                    const float* __restrict__ v,
+                                                    const uint8_t* __restrict__ mask,
+                                                    const uint8_t* __restrict__ finish, int N) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch || finish[b]) return;
+  const long long stride = (long long)batch * 6;
+  const float* rs = coords + 7 * stride + (long long)b * 6 + 3;
+  float3 last = make_float3(rs[0], rs[1], rs[2]);
+  coords[(long long)b * 6] = -1.f;
+  if (last.x < 0.f) return;
+  const float3 d = load3(v, b);
+  const float3 s = signs(d);
+  const float n = (float)N;
+  const long long cells = (long long)N * N * N;
+  int hits = 0;
+  while (hits < 8) {
+    float3 q;
+    float dt;
+    grid_step(last, d, s, q, dt);
+    if (outside_open(q, n)) {
+      coords[hits * stride + (long long)b * 6] = -1.f;
+      break;
+    }
+    if (occupied(mask, cell_index1(last, q, N), cells)) {
+      float* r = coords + hits * stride + (long long)b * 6;
+      r[0] = last.x;
+      r[1] = last.y;
+      r[2] = last.z;
+      r[3] = q.x;
+      r[4] = q.y;
+      r[5] = q.z;
+      ++hits;
+    }
+    last = q;
+  }
+}
+
+__global__ void pair_counts_kernel(int batch, const int* __restrict__ num, int* __restrict__ out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) out[b] = max(num[b] - 1, 0);
+}
+
+// ---- exclusive scan: int32 counts -> int64 offsets --------------------------
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ long long block_exclusive_scan(long long x, long long* smem, long long* total) {
+  // warp inclusive scan, then scan of warp totals
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long incl = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) smem[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = lane < (SCAN_THREADS / 32) ? smem[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < SCAN_THREADS / 32) smem[lane] = w;  // inclusive warp-total prefix
+  }
+  __syncthreads();
+  const long long warp_prefix = warp > 0 ? smem[warp - 1] : 0;
+  *total = smem[SCAN_THREADS / 32 - 1];
+  __syncthreads();
+  return warp_prefix + incl - x;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tile_sums(const int* __restrict__ in, long long n,
+                                                               long long* __restrict__ tile_sum) {
+  __shared__ long long smem[32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+  long long s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i)
+    if (base + i < n) s += in[base + i];
+  long long total;
+  block_exclusive_scan(s, smem, &total);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// Single block: exclusive scan of the tile sums in place.
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tile_prefix(long long* __restrict__ tile_sum, long long tiles) {
+  __shared__ long long smem[32];
+  long long carry = 0;
+  for (long long start = 0; start < tiles; start += SCAN_THREADS) {
+    const long long i = start + threadIdx.x;
+    const long long x = i < tiles ? tile_sum[i] : 0;
+    long long total;
+    const long long ex = block_exclusive_scan(x, smem, &total);
+    if (i < tiles) tile_sum[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) scan_tiles(const int* __restrict__ in, long long n,
+                                                           const long long* __restrict__ tile_prefix,
+                                                           int64_t* __restrict__ out) {
+  __shared__ long long smem[32];
+  const long long base = (long long)blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+  int vals[SCAN_ITEMS];
+  long long s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    vals[i] = base + i < n ? in[base + i] : 0;
+    s += vals[i];
+  }
+  long long total;
+  long long run = tile_prefix[blockIdx.x] + block_exclusive_scan(s, smem, &total);
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    if (base + i < n) out[base + i] = run;
+    run += vals[i];
+  }
+  if (base < n && base + SCAN_ITEMS >= n) out[n] = run;  // thread owning the last element
+}
+
+}  // namespace dv
+
+using namespace dv;
+
+// int(voxel_num * mask_scale) with the product rounded to float first, as the
+// reference computes it on the device (ray_voxel_intersect.cu:268).
+static int cells_per_side(float n, float scale) {
+  volatile float prod = n * scale;
+  return (int)prod;
+}
+
+static WalkArgs walk_args(int batch, float xyzmin, float n, float vs, float mask_scale,
+                          const float* o, const float* v, const uint8_t* mask) {
+  WalkArgs a{};
+  a.batch = batch;
+  a.xyzmin = xyzmin;
+  a.n = n;
+  a.voxel_size = vs;
+  a.mask_scale = mask_scale;
+  a.m = cells_per_side(n, mask_scale);
+  a.cells = (long long)a.m * a.m * a.m;
+  a.o = o;
+  a.v = v;
+  a.mask = mask;
+  return a;
+}
+
+extern "C" {
+
+int dv_ray_voxel_intersect(int batch_size, int max_n, float xyzmin, float xyzmax, float voxel_num,
+                           float voxel_size, const float* o, const float* v, float* intersection,
+                           int* intersect_num, float* tns, int* max_count, void* stream) {
+  (void)xyzmax;  // unused by the reference kernel as well
+  DV_CHECK(batch_size >= 0 && max_n >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && intersect_num && (max_n == 0 || (intersection && tns)), DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, 1.f, o, v, nullptr);
+  a.max_n = max_n;
+  a.inter = intersection;
+  a.num = intersect_num;
+  a.tns = tns;
+  a.max_count = max_count;
+  dense_walk_kernel<WALK_PADDED><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_ray_voxel_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                       const float* o, const float* v, int* intersect_num, int* max_count,
+                       void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && intersect_num, DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, 1.f, o, v, nullptr);
+  a.num = intersect_num;
+  a.max_count = max_count;
+  dense_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_masked_intersect(int batch_size, int max_n, float xyzmin, float xyzmax, float voxel_num,
+                        float voxel_size, float mask_scale, const float* o, const float* v,
+                        const uint8_t* mask, float* intersection, int* intersect_num, float* tns,
+                        int* max_count, void* stream) {
+  (void)xyzmax;
+  DV_CHECK(batch_size >= 0 && max_n >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && intersect_num && (max_n == 0 || (intersection && tns)), DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
+  a.max_n = max_n;
+  a.inter = intersection;
+  a.num = intersect_num;
+  a.tns = tns;
+  a.max_count = max_count;
+  masked_walk_kernel<WALK_PADDED><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                    float mask_scale, const float* o, const float* v, const uint8_t* mask,
+                    int* intersect_num, int* max_count, void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && intersect_num, DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
+  a.num = intersect_num;
+  a.max_count = max_count;
+  masked_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                       float mask_scale, const float* o, const float* v, const uint8_t* mask,
+                       const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
+                       void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
+  a.offsets = offsets;
+  a.seg = seg;
+  a.seg_t = seg_t;
+  a.seg_ray = seg_ray;
+  masked_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                      const float* o, const float* v, const int64_t* offsets, float* seg,
+                      float* seg_t, int* seg_ray, void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && offsets && seg, DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, 1.f, o, v, nullptr);
+  a.offsets = offsets;
+  a.seg = seg;
+  a.seg_t = seg_t;
+  a.seg_ray = seg_ray;
+  dense_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* seg_count, void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(intersect_num && seg_count, DV_ERR_ARG);
+  pair_counts_kernel<<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(batch_size, intersect_num, seg_count);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+long long dv_scan_scratch_bytes(long long n) {
+  const long long tiles = n > 0 ? (n + SCAN_TILE - 1) / SCAN_TILE : 1;
+  return tiles * (long long)sizeof(long long);
+}
+
+int dv_exclusive_scan(const int* counts, long long n, int64_t* offsets, void* scratch, void* stream) {
+  DV_CHECK(n >= 0 && offsets, DV_ERR_ARG);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    if (cudaMemsetAsync(offsets, 0, sizeof(int64_t), st) != cudaSuccess) return DV_ERR_CUDA;
+    return DV_OK;
+  }
+  DV_CHECK(counts && scratch, DV_ERR_ARG);
+  const long long tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+  DV_CHECK(tiles < (1LL << 31), DV_ERR_ARG);
+  long long* tile_sum = (long long*)scratch;
+  scan_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(counts, n, tile_sum);
+  scan_tile_prefix<<<1, SCAN_THREADS, 0, st>>>(tile_sum, tiles);
+  scan_tiles<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(counts, n, tile_sum, offsets);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_aabb_intersect(int batch_size, float* coords, const float* v, const float* center,
+                      uint8_t* finish, float* rgba, const uint8_t* octrees, int voxel_num,
+                      void* stream) {
+  DV_CHECK(batch_size >= 0 && voxel_num >= 64 && voxel_num % 64 == 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(coords && v && center && finish && rgba && octrees, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)rgba & 15) == 0, DV_ERR_ARG);
+  const long long a = voxel_num / 64, b = voxel_num / 16, c = voxel_num / 4;
+  const long long cells = a * a * a + b * b * b + c * c * c;
+  aabb_kernel<<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(
+      batch_size, coords, v, center, finish, rgba, octrees, voxel_num, cells);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_ray_march(int batch_size, float* coords, const float* v, const uint8_t* mask,
+                 const uint8_t* finish, int voxel_num, void* stream) {
+  DV_CHECK(batch_size >= 0 && voxel_num > 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(coords && v && mask && finish, DV_ERR_ARG);
+  march_kernel<<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(batch_size, coords, v, mask,
+                                                                           finish, voxel_num);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,178 @@
+"""DIVeR decoder parameters: the torch-form layers and their packed layouts.
+
+The decoder is the reference's pair of MLPs (model/diver.py:29-37,
+model/mlps.py:21-30):
+  mlp1: feature[C] -> hidden layers of width W -> (sigma, hidden[W])
+  mlp2: (hidden[W], PE(view dir)[27]) -> W -> rgb[3], then sigmoid
+with PE(d) = [d, sin(2^l pi d), cos(2^l pi d) for l in 0..3] (model/mlps.py:6-18).
+
+DIVeR32: mlp_point = [32, 2, 33], mlp_view = [32, 1]
+         (configs/nerf_synthetic_fine_diver32.py:118-127)
+DIVeR64: mlp_point = [64, 1, 65], mlp_view = [64, 1]
+         (configs/nerf_synthetic_fine.py:118-127)
+
+Packed torch form ("plain" layout, float32), used by the FP32 kernels: each
+Linear layer in order as W^T [in][out] row-major followed by its bias [out],
+each layer starting on a 4-float boundary.
+
+Real-time form: the reference's `convert.py` folding and flat `params` array
+(convert.py:59-140), see `pack_realtime`.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import torch
+
+KINDS = {
+    # kind: (width, mlp1 hidden layers)
+    "diver32": (32, 2),
+    "diver64": (64, 1),
+}
+PE_BANDS = 4
+PE_DIM = 3 + 3 * 2 * PE_BANDS  # 27
+
+
+@dataclass
+class Decoder:
+    kind: str
+    channels: int
+    layers: list = field(default_factory=list)  # [(weight [out,in], bias [out]), ...] mlp1 then mlp2
+
+    @property
+    def width(self) -> int:
+        return KINDS[self.kind][0]
+
+    @property
+    def n_mlp1(self) -> int:
+        return KINDS[self.kind][1] + 1
+
+    def to(self, device) -> "Decoder":
+        return Decoder(self.kind, self.channels, [(w.to(device), b.to(device)) for w, b in self.layers])
+
+    def dims(self) -> list[tuple[int, int]]:
+        return [(w.shape[1], w.shape[0]) for w, _ in self.layers]
+
+    def state_dict(self) -> dict:
+        """Names as in the reference's DIVeR module (mlp1.{0,2,4}, mlp2.{0,2})."""
+        sd = {}
+        for i, (w, b) in enumerate(self.layers[: self.n_mlp1]):
+            sd[f"mlp1.{2 * i}.weight"], sd[f"mlp1.{2 * i}.bias"] = w, b
+        for i, (w, b) in enumerate(self.layers[self.n_mlp1:]):
+            sd[f"mlp2.{2 * i}.weight"], sd[f"mlp2.{2 * i}.bias"] = w, b
+        return sd
+
+    @staticmethod
+    def from_state_dict(kind: str, sd: dict) -> "Decoder":
+        width, depth = KINDS[kind]
+        layers = [(sd[f"mlp1.{2 * i}.weight"], sd[f"mlp1.{2 * i}.bias"]) for i in range(depth + 1)]
+        layers += [(sd[f"mlp2.{2 * i}.weight"], sd[f"mlp2.{2 * i}.bias"]) for i in range(2)]
+        return Decoder(kind, layers[0][0].shape[1], [(w.float(), b.float()) for w, b in layers])
+
+
+def layer_dims(kind: str, channels: int) -> list[tuple[int, int]]:
+    width, depth = KINDS[kind]
+    dims = [(channels, width)] + [(width, width)] * (depth - 1) + [(width, width + 1)]
+    dims += [(width + PE_DIM, width), (width, 3)]
+    return dims
+
+
+def random_decoder(kind: str, channels: int, seed: int) -> Decoder:
+    """Default nn.Linear initialisation (Kaiming-uniform, a=sqrt(5)) under manual_seed(seed), CPU."""
+    g = torch.Generator().manual_seed(seed)
+    layers = []
+    for fin, fout in layer_dims(kind, channels):
+        bound = 1.0 / math.sqrt(fin)
+        # kaiming_uniform_(a=sqrt(5)) on [out, in] gives U(-1/sqrt(in), 1/sqrt(in))
+        w = (torch.rand(fout, fin, generator=g) * 2 - 1) * bound
+        b = (torch.rand(fout, generator=g) * 2 - 1) * bound
+        layers.append((w, b))
+    return Decoder(kind, channels, layers)
+
+
+def plain_layout(kind: str, channels: int) -> list[tuple[int, int, int, int]]:
+    """[(in, out, weight_offset, bias_offset)] of the packed torch form."""
+    out = []
+    off = 0
+    for fin, fout in layer_dims(kind, channels):
+        w_off = off
+        b_off = w_off + fin * fout
+        off = b_off + fout
+        off = (off + 3) // 4 * 4
+        out.append((fin, fout, w_off, b_off))
+    return out
+
+
+def plain_size(kind: str, channels: int) -> int:
+    fin, fout, w_off, b_off = plain_layout(kind, channels)[-1]
+    return (b_off + fout + 3) // 4 * 4
+
+
+def pack_plain(dec: Decoder) -> torch.Tensor:
+    lay = plain_layout(dec.kind, dec.channels)
+    flat = torch.zeros(plain_size(dec.kind, dec.channels), dtype=torch.float32)
+    for (w, b), (fin, fout, w_off, b_off) in zip(dec.layers, lay):
+        flat[w_off:w_off + fin * fout] = w.detach().float().cpu().t().reshape(-1)
+        flat[b_off:b_off + fout] = b.detach().float().cpu()
+    return flat
+
+
+def unpack_plain_grad(kind: str, channels: int, flat: torch.Tensor) -> list[tuple[torch.Tensor, torch.Tensor]]:
+    """Gradients in the packed layout -> [(dW [out,in], db [out])]."""
+    res = []
+    for fin, fout, w_off, b_off in plain_layout(kind, channels):
+        dw = flat[w_off:w_off + fin * fout].reshape(fin, fout).t().contiguous()
+        db = flat[b_off:b_off + fout].clone()
+        res.append((dw, db))
+    return res
+
+
+# --- real-time form (convert.py) ---------------------------------------------
+
+# Column order of the folded PE weights: per axis [d, sin x4, cos x4]
+# (convert.py:89-92,128-131).
+PE_REORDER = [0, 3, 9, 15, 21, 6, 12, 18, 24,
+              1, 4, 10, 16, 22, 7, 13, 19, 25,
+              2, 5, 11, 17, 23, 8, 14, 20, 26]
+REALTIME_PARAMS = {"diver32": 3168, "diver64": 8288}
+
+
+def pack_realtime(dec: Decoder) -> torch.Tensor:
+    """The flat `params` array of the reference's serialized model
+    (convert.py:63-140): the activation-free sigma/hidden layer is folded into
+    mlp2's first layer, PE columns reordered, 28 zeros of padding.  DIVeR32's
+    first layer (weightin) keeps only its bias here; its matrix is applied to
+    the feature table at conversion time (`premultiply_features`)."""
+    L = [(w.detach().float().cpu(), b.detach().float().cpu()) for w, b in dec.layers]
+    W = dec.width
+    if dec.kind == "diver32":
+        (w01, b01), (w11, b11), (w21, b21), (w22, b22), (w3, b3) = L
+        head = [b01]
+        mid = [torch.cat([b11[:, None], w11], 1).t().reshape(-1)]
+    else:
+        (w1, b1), (w21, b21), (w22, b22), (w3, b3) = L
+        head = []
+        mid = [torch.cat([b1[:, None], w1], 1).t().reshape(-1)]
+    lin40, bias40 = w21[:1], b21[:1]
+    lin41 = w22[:, :W] @ w21[1:]
+    bias41 = w22[:, :W] @ b21[1:] + b22
+    lin42 = w22[:, W:]
+    lin4 = torch.cat([lin40, lin41], 0)
+    bias4 = torch.cat([bias40, bias41], 0)
+    weight1 = torch.cat([bias4[0, None], lin4[0]], 0)
+    w2 = torch.cat([bias4[1:, None], lin4[1:], lin42], 1)
+    w2 = torch.cat([w2[:, :-PE_DIM], w2[:, -PE_DIM:][:, PE_REORDER]], -1)
+    weight3 = torch.cat([b3[:, None], w3], -1)
+    params = torch.cat(head + mid + [weight1.reshape(-1), w2.t().reshape(-1), weight3.t().reshape(-1), torch.zeros(28)], 0)
+    assert params.numel() == REALTIME_PARAMS[dec.kind], params.numel()
+    return params.contiguous()
+
+
+def premultiply_features(dec: Decoder, features: torch.Tensor) -> torch.Tensor:
+    """DIVeR32 stores features already multiplied by its first layer's matrix
+    (convert.py:148-150); DIVeR64 stores them as they are."""
+    if dec.kind == "diver32":
+        w01 = dec.layers[0][0].to(features.device, torch.float32)
+        return (features @ w01.t()).contiguous()
+    return features.contiguous()

@@ -1,0 +1,184 @@
+"""Ray–voxel traversal operators with the reference's interface.
+
+Drop-in for utils/ray_voxel_intersection/__init__.py (reference :18-87):
+`ray_voxel_intersect(o, v, xyzmin, xyzmax, voxel_num, voxel_size)` and
+`masked_intersect(o, v, xyzmin, xyzmax, voxel_num, voxel_size, mask, mask_scale)`
+return `(intersection[:, :K], tns >= 0, tns[:, :K])` with K = max count, the
+same values the reference returns.  The reference fills [B, 3N] padded buffers
+and slices them; here a counting walk finds K first (the same single host
+read of max(count) the reference does) and the filling walk writes [B, K]
+rows only.
+
+`masked_segments` / `dense_segments` return the compacted segment lists that
+DIVeR.extract_features builds from those buffers by boolean indexing
+(model/diver.py:86-103), without the padded intermediate.
+"""
+from __future__ import annotations
+
+import torch
+from torch.autograd import Function
+
+from . import _native as N
+
+
+def _check_rays(o: torch.Tensor, v: torch.Tensor) -> int:
+    N.need_cuda("o", o, torch.float32)
+    N.need_cuda("v", v, torch.float32)
+    if o.dim() != 2 or o.shape[1] != 3 or v.shape != o.shape:
+        raise ValueError(f"o and v must be [B, 3] with equal shapes, got {tuple(o.shape)} and {tuple(v.shape)}")
+    if o.device != v.device:
+        raise ValueError("o and v must be on the same device")
+    return o.shape[0]
+
+
+def mask_side(voxel_num: float, mask_scale: float) -> int:
+    """int(voxel_num * mask_scale) with the product rounded to float32, as the reference computes it."""
+    return int(torch.tensor(float(voxel_num), dtype=torch.float32).mul(float(mask_scale)).item())
+
+
+def _check_mask(mask: torch.Tensor, voxel_num: float, mask_scale: float) -> torch.Tensor:
+    N.need_cuda("mask", mask)
+    if mask.dtype not in (torch.bool, torch.uint8):
+        raise TypeError(f"mask must be bool or uint8, got {mask.dtype}")
+    m = mask_side(voxel_num, mask_scale)
+    if mask.numel() != m * m * m:
+        raise ValueError(f"mask must hold {m}^3 cells for voxel_num={voxel_num}, mask_scale={mask_scale}; got {tuple(mask.shape)}")
+    return mask.view(torch.uint8) if mask.dtype == torch.bool else mask
+
+
+def _max_count(counter: torch.Tensor) -> int:
+    return int(counter.item())
+
+
+class RayVoxelIntersect(Function):
+    @staticmethod
+    def forward(ctx, o, v, xyzmin, xyzmax, voxel_num, voxel_size):
+        """Dense traversal (reference utils/ray_voxel_intersection/__init__.py:19-43).
+        Returns B x K x 3 points, B x K hit indicator, B x K distances."""
+        B = _check_rays(o, v)
+        dev = o.device
+        st = N.stream(dev)
+        num = torch.empty(B, dtype=torch.int32, device=dev)
+        mx = torch.zeros(1, dtype=torch.int32, device=dev)
+        N.call("dv_ray_voxel_count", B, float(xyzmin), float(voxel_num), float(voxel_size),
+               N.ptr(o), N.ptr(v), N.ptr(num), N.ptr(mx), st)
+        K = _max_count(mx)
+        inter = torch.zeros(B, K, 3, dtype=torch.float32, device=dev)
+        tns = torch.full((B, K), -1.0, dtype=torch.float32, device=dev)
+        if K > 0:
+            N.call("dv_ray_voxel_intersect", B, K, float(xyzmin), float(xyzmax), float(voxel_num),
+                   float(voxel_size), N.ptr(o), N.ptr(v), N.ptr(inter), N.ptr(num), N.ptr(tns), None, st)
+        return inter, tns >= 0, tns
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None
+
+
+class MaskedIntersect(Function):
+    @staticmethod
+    def forward(ctx, o, v, xyzmin, xyzmax, voxel_num, voxel_size, mask, mask_scale):
+        """Masked traversal (reference utils/ray_voxel_intersection/__init__.py:51-79).
+        Returns B x K x 6 (entry, exit), B x K hit indicator, B x K exit distances."""
+        B = _check_rays(o, v)
+        m8 = _check_mask(mask, voxel_num, mask_scale)
+        dev = o.device
+        st = N.stream(dev)
+        num = torch.empty(B, dtype=torch.int32, device=dev)
+        mx = torch.zeros(1, dtype=torch.int32, device=dev)
+        N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), st)
+        K = _max_count(mx)
+        inter = torch.zeros(B, K, 6, dtype=torch.float32, device=dev)
+        tns = torch.full((B, K), -1.0, dtype=torch.float32, device=dev)
+        if K > 0:
+            N.call("dv_masked_intersect", B, K, float(xyzmin), float(xyzmax), float(voxel_num),
+                   float(voxel_size), float(mask_scale), N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(inter),
+                   N.ptr(num), N.ptr(tns), None, st)
+        return inter, tns >= 0, tns
+
+    @staticmethod
+    def backward(ctx, a, b, c):
+        return None, None, None, None, None, None, None, None
+
+
+ray_voxel_intersect = RayVoxelIntersect.apply
+masked_intersect = MaskedIntersect.apply
+
+
+def exclusive_scan(counts: torch.Tensor) -> torch.Tensor:
+    """int32 counts [n] -> int64 offsets [n+1] on the device (no host sync)."""
+    N.need_cuda("counts", counts, torch.int32)
+    n = counts.numel()
+    out = torch.empty(n + 1, dtype=torch.int64, device=counts.device)
+    scratch = torch.empty(max(int(N.lib().dv_scan_scratch_bytes(n)), 8), dtype=torch.uint8, device=counts.device)
+    N.call("dv_exclusive_scan", N.ptr(counts), n, N.ptr(out), N.ptr(scratch), N.stream(counts.device))
+    return out
+
+
+class Segments:
+    """Compacted per-ray segment lists (CSR).
+
+    offsets [B+1] int64, seg [S, 6] float32 (entry xyz, exit xyz, voxel units),
+    t [S] float32 distances, ray [S] int32 ray index, counts [B] int32.
+    """
+
+    __slots__ = ("offsets", "seg", "t", "ray", "counts")
+
+    def __init__(self, offsets, seg, t, ray, counts):
+        self.offsets, self.seg, self.t, self.ray, self.counts = offsets, seg, t, ray, counts
+
+    @property
+    def coord_in(self) -> torch.Tensor:
+        return self.seg[:, :3]
+
+    @property
+    def coord_out(self) -> torch.Tensor:
+        return self.seg[:, 3:]
+
+    @property
+    def total(self) -> int:
+        return self.seg.shape[0]
+
+
+def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale) -> Segments:
+    """Segments of occupied voxels; equals coord[mask] of masked_intersect's output
+    (model/diver.py:86-93), t = exit distance."""
+    B = _check_rays(o, v)
+    m8 = _check_mask(mask, voxel_num, mask_scale)
+    dev = o.device
+    st = N.stream(dev)
+    num = torch.empty(B, dtype=torch.int32, device=dev)
+    N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), None, st)
+    offsets = exclusive_scan(num)
+    S = int(offsets[-1].item())
+    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
+    t = torch.empty(S, dtype=torch.float32, device=dev)
+    ray = torch.empty(S, dtype=torch.int32, device=dev)
+    if S > 0:
+        N.call("dv_masked_segments", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
+    return Segments(offsets, seg, t, ray, num)
+
+
+def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
+    """Consecutive crossing points paired into segments; equals
+    (coord[:, :-1][mask], coord[:, 1:][mask]) of model/diver.py:95-103, t = entry distance."""
+    B = _check_rays(o, v)
+    dev = o.device
+    st = N.stream(dev)
+    num = torch.empty(B, dtype=torch.int32, device=dev)
+    N.call("dv_ray_voxel_count", B, float(xyzmin), float(voxel_num), float(voxel_size),
+           N.ptr(o), N.ptr(v), N.ptr(num), None, st)
+    pairs = torch.empty_like(num)
+    N.call("dv_dense_pair_counts", B, N.ptr(num), N.ptr(pairs), st)
+    offsets = exclusive_scan(pairs)
+    S = int(offsets[-1].item())
+    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
+    t = torch.empty(S, dtype=torch.float32, device=dev)
+    ray = torch.empty(S, dtype=torch.int32, device=dev)
+    if S > 0:
+        N.call("dv_dense_segments", B, float(xyzmin), float(voxel_num), float(voxel_size),
+               N.ptr(o), N.ptr(v), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
+    return Segments(offsets, seg, t, ray, pairs)

@@ -1,0 +1,167 @@
+/*
+ * diver_gb300 — C ABI of the GB300 (sm_103a) DIVeR rendering hot path.
+ *
+ * Every entry point takes plain device pointers, sizes and scalars, plus the
+ * CUDA stream to launch on (passed as void*, NULL = legacy default stream),
+ * and returns a dv_status.  No entry point synchronises the device, exits the
+ * process, or allocates memory unless its comment says so; output buffers are
+ * owned by the caller.  All launches are stream-ordered.
+ *
+ * Coordinates are in voxel units (a point p in world space maps to
+ * (p - xyzmin) / voxel_size).  Grids are stored [z][y][x][channel] with x
+ * fastest, exactly as the reference's `voxels` parameter (model/diver.py:37).
+ *
+ * Reference citations are to files of the DIVeR project (lwwu2/diver).
+ */
+#ifndef DIVER_GB300_H
+#define DIVER_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define DV_API __attribute__((visibility("default")))
+#else
+#define DV_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum dv_status {
+  DV_OK = 0,
+  DV_ERR_ARG = 1,       /* bad size, NULL pointer or unsupported option */
+  DV_ERR_CUDA = 2,      /* a CUDA call or launch failed */
+  DV_ERR_OOM = 3,       /* an allocation (only in entry points that allocate) failed */
+  DV_ERR_TIMEOUT = 4,   /* a bounded device wait ran out; see dv_last_device_error */
+  DV_ERR_OVERFLOW = 5,  /* a capacity given by the caller was too small */
+  DV_ERR_UNSUPPORTED = 6 /* the device is not sm_103 / feature not compiled */
+} dv_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+DV_API int dv_version(void);
+
+/* Name of a status code (static string). */
+DV_API const char* dv_status_string(int status);
+
+/* ------------------------------------------------------------------------
+ * Ray–voxel traversal, training/offline path.
+ * ------------------------------------------------------------------------ */
+
+/*
+ * Dense 3D-DDA: records the entry point of each ray into [0,N]^3 and every
+ * grid-plane crossing after it.
+ * Replaces ray_voxel_intersect_wrapper
+ *   (utils/ray_voxel_intersection/src/ray_voxel_intersect.cu:154-172)
+ * and the kernel it launches (same file :29-151).
+ *   o, v          [batch][3] ray origins (world) and unit directions
+ *   intersection  [batch][max_n][3]; the caller fills it with 0
+ *   intersect_num [batch]; written (not accumulated)
+ *   tns           [batch][max_n]; the caller fills it with -1
+ *   max_count     optional device int (NULL to skip) that receives
+ *                 max(intersect_num) through atomicMax; the caller zeroes it
+ * Points beyond max_n are counted but not stored (the reference writes past
+ * its buffer in that case).  As in the reference, a missed ray still gets its
+ * clamped slab point in row 0 with count 0 and tns -1.
+ */
+DV_API int dv_ray_voxel_intersect(int batch_size, int max_n, float xyzmin, float xyzmax,
+                           float voxel_num, float voxel_size, const float* o, const float* v,
+                           float* intersection, int* intersect_num, float* tns, int* max_count,
+                           void* stream);
+
+/* Count-only pass of dv_ray_voxel_intersect (same walk, nothing stored but
+ * intersect_num and max_count). */
+DV_API int dv_ray_voxel_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                       const float* o, const float* v, int* intersect_num, int* max_count,
+                       void* stream);
+
+/*
+ * Masked 3D-DDA: records (entry, exit) of every voxel whose occupancy byte is
+ * set, with the exit distance in tns.
+ * Replaces masked_intersect_wrapper
+ *   (utils/ray_voxel_intersection/src/ray_voxel_intersect.cu:323-341)
+ * and masked_intersect_kernel (same file :192-319).
+ *   mask          [M][M][M] bytes, M = int(voxel_num * mask_scale)
+ *   intersection  [batch][max_n][6]; caller fills with 0
+ *   tns           [batch][max_n]; caller fills with -1
+ */
+DV_API int dv_masked_intersect(int batch_size, int max_n, float xyzmin, float xyzmax, float voxel_num,
+                        float voxel_size, float mask_scale, const float* o, const float* v,
+                        const uint8_t* mask, float* intersection, int* intersect_num, float* tns,
+                        int* max_count, void* stream);
+
+/* Count-only pass of dv_masked_intersect. */
+DV_API int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                    float mask_scale, const float* o, const float* v, const uint8_t* mask,
+                    int* intersect_num, int* max_count, void* stream);
+
+/*
+ * Compacted (CSR) segment lists, the form DIVeR.extract_features builds with
+ * boolean indexing (model/diver.py:86-103).  offsets[batch+1] is the exclusive
+ * scan of the per-ray segment counts.  For every ray b, its segments are
+ * written to rows offsets[b] .. offsets[b+1]-1 of
+ *   seg      [S][6]  (entry xyz, exit xyz) in voxel units
+ *   seg_t    [S]     distance (world units) or NULL
+ *   seg_ray  [S]     ray index or NULL
+ * Masked: one segment per occupied voxel, seg_t = exit distance (the masked
+ *   kernel's tns).  Counts come from dv_masked_count.
+ * Dense: consecutive crossing points pair into segments; ray b has
+ *   max(count-1, 0) segments and seg_t is the entry distance (model/diver.py:
+ *   95-103).  Counts come from dv_ray_voxel_count (minus one per ray).
+ */
+DV_API int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                       float mask_scale, const float* o, const float* v, const uint8_t* mask,
+                       const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
+                       void* stream);
+DV_API int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                      const float* o, const float* v, const int64_t* offsets, float* seg,
+                      float* seg_t, int* seg_ray, void* stream);
+
+/* Per-ray segment counts for the dense pairing: max(intersect_num - 1, 0). */
+DV_API int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* seg_count, void* stream);
+
+/*
+ * Exclusive prefix sum of n int32 counts into n+1 int64 offsets
+ * (offsets[n] = total).  scratch must hold dv_scan_scratch_bytes(n) bytes.
+ */
+DV_API long long dv_scan_scratch_bytes(long long n);
+DV_API int dv_exclusive_scan(const int* counts, long long n, int64_t* offsets, void* scratch,
+                      void* stream);
+
+/* ------------------------------------------------------------------------
+ * Real-time path: occupancy-octree first hit and 8-hit ray march.
+ * ------------------------------------------------------------------------ */
+
+/*
+ * First occupied 4^3 block of each pixel's ray through three max-pooled
+ * occupancy levels (N/64, N/16, N/4).  Replaces aabb_intersect_wrapper
+ *   (utils/ray_march/src/ray_march.cu:237-266) and aabb_intersect_kernel
+ *   (same file :24-149).
+ *   coords   [8][batch][6] hit buffer; slot 7 [3:6] receives the resume point
+ *            (x = -1 on a miss)
+ *   v        [batch][3] unit directions
+ *   center   [3] camera centre in voxel units (device pointer)
+ *   finish   [batch] bytes; set to 1 on a miss, else 0
+ *   rgba     [batch][4]; initialised to (0,0,0,1)
+ *   octrees  bytes, levels (N/64)^3, (N/16)^3, (N/4)^3 concatenated
+ *   voxel_num  N, a multiple of 64
+ */
+DV_API int dv_aabb_intersect(int batch_size, float* coords, const float* v, const float* center,
+                      uint8_t* finish, float* rgba, const uint8_t* octrees, int voxel_num,
+                      void* stream);
+
+/*
+ * Records the next (up to) 8 occupied voxels of every unfinished ray into
+ * coords[hit][b][0:6], resuming from coords[7][b][3:6]; a ray that leaves the
+ * grid gets x = -1 in the slot after its last hit.  Replaces ray_march_wrapper
+ *   (utils/ray_march/src/ray_march.cu:268-296) and ray_march_kernel (:151-230).
+ *   mask  [N][N][N] occupancy bytes
+ */
+DV_API int dv_ray_march(int batch_size, float* coords, const float* v, const uint8_t* mask,
+                 const uint8_t* finish, int voxel_num, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIVER_GB300_H */

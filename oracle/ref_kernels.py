@@ -1,0 +1,154 @@
+"""ORACLE — test infrastructure only.  The reference's own CUDA traversal
+kernels, compiled from the reference sources in place and run through the
+CUDA driver API, to produce the traversal fixtures in tests/golden/.
+
+  build_cubins()  nvcc -cubin of utils/ray_voxel_intersection/src/
+                  ray_voxel_intersect.cu and utils/ray_march/src/ray_march.cu
+                  with the reference's default nvcc flags (no fast math,
+                  default -fmad=true) into oracle/_ref/*.cubin.  Needs the
+                  reference tree; oracle/ref_shim/ supplies a stand-in for its
+                  torch-dependent cuda_utils.h.
+  RefKernels      loads the cubins (libcuda via ctypes) and launches
+                  ray_voxel_intersect_kernel, masked_intersect_kernel,
+                  aabb_intersect_kernel<N> and ray_march_kernel<N> with the
+                  launch shapes of the reference wrappers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+REF_ROOT = Path(os.environ.get("DIVER_REFERENCE", "/root/reference"))
+OUT = HERE / "_ref"
+UNITS = {
+    "ray_voxel_intersect": "utils/ray_voxel_intersection/src/ray_voxel_intersect.cu",
+    "ray_march": "utils/ray_march/src/ray_march.cu",
+}
+
+
+def build_cubins(force: bool = False) -> list[Path]:
+    """Compiles the reference kernels when the reference sources are present."""
+    out = []
+    for name, rel in UNITS.items():
+        src = REF_ROOT / rel
+        dst = OUT / f"{name}.cubin"
+        if not src.exists():
+            continue
+        if dst.exists() and not force and dst.stat().st_mtime >= src.stat().st_mtime:
+            out.append(dst)
+            continue
+        OUT.mkdir(parents=True, exist_ok=True)
+        inc = src.parent.parent / "include"
+        cmd = ["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
+               "-I", str(HERE / "ref_shim"), "-I", str(inc), str(src), "-o", str(dst)]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference cubin build failed for {rel}:\n{r.stdout.decode(errors='replace')}")
+        out.append(dst)
+    return out
+
+
+class _Driver:
+    def __init__(self):
+        self.cu = C.CDLL("libcuda.so.1")
+
+    def check(self, res, what):
+        if res != 0:
+            raise RuntimeError(f"{what} failed with CUresult {res}")
+
+
+class RefKernels:
+    """The reference traversal kernels, launched on torch's current stream."""
+
+    def __init__(self):
+        import torch
+
+        torch.zeros(1, device="cuda")  # make the primary context current
+        self.d = _Driver()
+        self.mods = {}
+        self.funcs = {}
+        for name in UNITS:
+            path = OUT / f"{name}.cubin"
+            if not path.exists():
+                raise FileNotFoundError(f"{path} missing: build it with oracle.ref_kernels.build_cubins() where the reference sources are present")
+            mod = C.c_void_p()
+            self.d.check(self.d.cu.cuModuleLoad(C.byref(mod), str(path).encode()), f"cuModuleLoad({path.name})")
+            self.mods[name] = mod
+            cnt = C.c_uint()
+            self.d.check(self.d.cu.cuModuleGetFunctionCount(C.byref(cnt), mod), "cuModuleGetFunctionCount")
+            arr = (C.c_void_p * cnt.value)()
+            self.d.check(self.d.cu.cuModuleEnumerateFunctions(arr, cnt, mod), "cuModuleEnumerateFunctions")
+            for f in arr:
+                nm = C.c_char_p()
+                self.d.check(self.d.cu.cuFuncGetName(C.byref(nm), C.c_void_p(f)), "cuFuncGetName")
+                self.funcs[nm.value.decode()] = C.c_void_p(f)
+
+    def _func(self, needle: str, extra: str = ""):
+        for k, f in self.funcs.items():
+            if needle in k and extra in k:
+                return f
+        raise KeyError(f"kernel {needle} {extra} not in {list(self.funcs)}")
+
+    def _launch(self, f, grid, block, args):
+        import torch
+
+        holders = []
+        ptrs = (C.c_void_p * len(args))()
+        for i, a in enumerate(args):
+            if isinstance(a, torch.Tensor):
+                h = C.c_void_p(a.data_ptr())
+            elif isinstance(a, float):
+                h = C.c_float(a)
+            else:
+                h = C.c_int(int(a))
+            holders.append(h)
+            ptrs[i] = C.cast(C.byref(h), C.c_void_p)
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self.d.check(self.d.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, 0, st, ptrs, None), "cuLaunchKernel")
+        torch.cuda.synchronize()
+
+    def dense(self, o, v, xyzmin, xyzmax, voxel_num, voxel_size):
+        """ray_voxel_intersect wrapper semantics (ray_voxel_intersect.cpp:13-42)."""
+        import torch
+
+        B = o.shape[0]
+        max_n = int(float(voxel_num) * 3)
+        inter = torch.zeros(B, max_n, 3, device="cuda")
+        num = torch.zeros(B, dtype=torch.int32, device="cuda")
+        tns = torch.full((B, max_n), -1.0, device="cuda")
+        self._launch(self._func("ray_voxel_intersect_kernel"), (B + 1023) // 1024, 1024,
+                     [B, max_n, float(xyzmin), float(xyzmax), float(voxel_num), float(voxel_size), o, v, inter, num, tns])
+        return inter, num, tns
+
+    def masked(self, o, v, xyzmin, xyzmax, voxel_num, voxel_size, mask, mask_scale):
+        import torch
+
+        B = o.shape[0]
+        max_n = int(float(voxel_num) * 3)
+        inter = torch.zeros(B, max_n, 6, device="cuda")
+        num = torch.zeros(B, dtype=torch.int32, device="cuda")
+        tns = torch.full((B, max_n), -1.0, device="cuda")
+        self._launch(self._func("masked_intersect_kernel"), (B + 1023) // 1024, 1024,
+                     [B, max_n, float(xyzmin), float(xyzmax), float(voxel_num), float(voxel_size), float(mask_scale),
+                      o, v, mask, inter, num, tns])
+        return inter, num, tns
+
+    def aabb(self, o, v, center, finish, rgba, octrees, N):
+        import torch
+
+        g = C.c_void_p()
+        size = C.c_size_t()
+        self.d.check(self.d.cu.cuModuleGetGlobal_v2(C.byref(g), C.byref(size), self.mods["ray_march"], b"c_center"),
+                     "cuModuleGetGlobal(c_center)")
+        c = center.detach().float().cpu().contiguous()
+        self.d.check(self.d.cu.cuMemcpyHtoD_v2(g, C.c_void_p(c.data_ptr()), C.c_size_t(12)), "cuMemcpyHtoD")
+        B = v.numel() // 3
+        self._launch(self._func("aabb_intersect_kernel", f"ILi{N}E"), (B + 1023) // 1024, 1024,
+                     [B, o, v, finish, rgba, octrees])
+
+    def march(self, o, v, mask, finish, N):
+        B = v.numel() // 3
+        self._launch(self._func("ray_march_kernel", f"ILi{N}E"), 256, 1024, [B, o, v, mask, finish])
