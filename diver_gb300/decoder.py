@@ -12,8 +12,9 @@ DIVeR64: mlp_point = [64, 1, 65], mlp_view = [64, 1]
          (configs/nerf_synthetic_fine.py:118-127)
 
 Packed torch form ("plain" layout, float32), used by the FP32 kernels: each
-Linear layer in order as W^T [in][out] row-major followed by its bias [out],
-each layer starting on a 4-float boundary.
+Linear layer in order as W^T [in][out4] row-major (out4 = out rounded up to a
+multiple of 4, extra columns zero) followed by its bias [out4], so every row
+is a whole number of float4s.
 
 Real-time form: the reference's `convert.py` folding and flat `params` array
 (convert.py:59-140), see `pack_realtime`.
@@ -91,29 +92,34 @@ def random_decoder(kind: str, channels: int, seed: int) -> Decoder:
     return Decoder(kind, channels, layers)
 
 
+def pad4(n: int) -> int:
+    return (n + 3) // 4 * 4
+
+
 def plain_layout(kind: str, channels: int) -> list[tuple[int, int, int, int]]:
-    """[(in, out, weight_offset, bias_offset)] of the packed torch form."""
+    """[(in, out, weight_offset, bias_offset)] of the packed torch form; rows are pad4(out) long."""
     out = []
     off = 0
     for fin, fout in layer_dims(kind, channels):
         w_off = off
-        b_off = w_off + fin * fout
-        off = b_off + fout
-        off = (off + 3) // 4 * 4
+        b_off = w_off + fin * pad4(fout)
+        off = b_off + pad4(fout)
         out.append((fin, fout, w_off, b_off))
     return out
 
 
 def plain_size(kind: str, channels: int) -> int:
     fin, fout, w_off, b_off = plain_layout(kind, channels)[-1]
-    return (b_off + fout + 3) // 4 * 4
+    return b_off + pad4(fout)
 
 
 def pack_plain(dec: Decoder) -> torch.Tensor:
     lay = plain_layout(dec.kind, dec.channels)
     flat = torch.zeros(plain_size(dec.kind, dec.channels), dtype=torch.float32)
     for (w, b), (fin, fout, w_off, b_off) in zip(dec.layers, lay):
-        flat[w_off:w_off + fin * fout] = w.detach().float().cpu().t().reshape(-1)
+        wt = torch.zeros(fin, pad4(fout))
+        wt[:, :fout] = w.detach().float().cpu().t()
+        flat[w_off:w_off + fin * pad4(fout)] = wt.reshape(-1)
         flat[b_off:b_off + fout] = b.detach().float().cpu()
     return flat
 
@@ -122,7 +128,7 @@ def unpack_plain_grad(kind: str, channels: int, flat: torch.Tensor) -> list[tupl
     """Gradients in the packed layout -> [(dW [out,in], db [out])]."""
     res = []
     for fin, fout, w_off, b_off in plain_layout(kind, channels):
-        dw = flat[w_off:w_off + fin * fout].reshape(fin, fout).t().contiguous()
+        dw = flat[w_off:w_off + fin * pad4(fout)].reshape(fin, pad4(fout))[:, :fout].t().contiguous()
         db = flat[b_off:b_off + fout].clone()
         res.append((dw, db))
     return res

@@ -129,6 +129,36 @@ DV_API int dv_exclusive_scan(const int* counts, long long n, int64_t* offsets, v
                       void* stream);
 
 /* ------------------------------------------------------------------------
+ * Feature integration.
+ * ------------------------------------------------------------------------ */
+
+/*
+ * Mean of the trilinear interpolant of the 8 corner vectors over each
+ * segment (closed form).  Replaces the reference's torch `integrate`
+ * (utils/integrator.py:62-112).
+ *   voxels    [nvz][nvy][nvx][channels] corner features, 16-byte aligned,
+ *             channels a multiple of 4
+ *   coord_i/o entry / exit points, 3 floats per row, rows coord_stride floats
+ *             apart (3 for separate [S,3] arrays, 6 for the halves of [S,6])
+ *   feature   [n_seg][channels] output
+ * The lower corner is min(int(p_in + 1e-4), int(p_out + 1e-4)) per axis and
+ * the upper corner is clamped to the last vertex, as in the reference.
+ */
+DV_API int dv_integrate_fwd(const float* voxels, int nvx, int nvy, int nvz, int channels,
+                            const float* coord_i, const float* coord_o, long long coord_stride,
+                            long long n_seg, float* feature, void* stream);
+
+/*
+ * Gradient of dv_integrate_fwd with respect to the corner features:
+ * grad_voxels[corner] += w_corner * grad_feature, accumulated with atomics
+ * (the caller zeroes grad_voxels).  This is the scatter the reference's
+ * autograd performs through its 8 gathers (utils/integrator.py:80-85).
+ */
+DV_API int dv_integrate_bwd(const float* grad_feature, int nvx, int nvy, int nvz, int channels,
+                            const float* coord_i, const float* coord_o, long long coord_stride,
+                            long long n_seg, float* grad_voxels, void* stream);
+
+/* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.
  * ------------------------------------------------------------------------ */
 
