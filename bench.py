@@ -1,0 +1,409 @@
+#!/usr/bin/env python
+"""Benchmark of the DIVeR hot path on GB300.
+
+Default workload (one step): one training forward + backward over a batch of
+4096 rays of the 256^3 x 32-channel DIVeR32 scene (257^3 corner features,
+~60% occupancy), rays drawn from 100 cameras at 800x800 among rays that hit
+occupied voxels, MSE + sparsity loss, gradients for the feature grid and the
+decoder.  Inputs are synthetic (seeded), with the shapes of the reference's
+NeRF-synthetic fine configuration.  Also reported: full-frame render
+(800x800) rays/s and p50/p99 frame latency on the same scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the reference algorithm on the host cores (the CPU
+oracle: C traversal + torch CPU integrate/decoder/render/loss with autograd),
+on bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mrays/s render & train fwd+bwd, p50/p99 frame ms; fused BF16 vs plain FP32 @ tol"
+BATCH = 4096
+L_S = 1e-5
+# Algorithmic FLOPs per segment (2 x multiply-adds), DIVeR32 with 32 channels:
+#   decoder forward  4224 MACs (mlp1 3 layers, mlp2 hidden part + output; the PE
+#                    part of mlp2's first layer is per ray) + 256 (integral)
+#   decoder backward 4224 (input grads) + 5088 (weight grads incl. PE rows)
+#                    + 256 (integral) + 256 (corner scatter) + 4224 (recompute)
+FLOP_PER_SEG = {"dv_decode_fwd": 2 * (4224 + 256), "dv_decode_bwd": 2 * (4224 + 5088 + 256 + 256 + 4224 + 256)}
+OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd, composite_fwd, composite_bwd, decode_bwd
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--frames", type=int, default=8)
+    p.add_argument("--no-render", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(n):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allreduce_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples (every 200 ms) during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --- workload ------------------------------------------------------------------
+
+def train_scene(device):
+    from diver_gb300 import scenes
+
+    return scenes.grid_scene(256, 32, "diver32", device=device)
+
+
+def make_batches(scene, count, device, seed=4):
+    """`count` batches of BATCH rays from 100 cameras at 800x800 (focal 960),
+    kept only where the ray crosses at least one occupied voxel."""
+    import torch
+
+    from diver_gb300 import _native as N
+    from diver_gb300 import scenes
+
+    cams = scenes.sphere_cameras(100, 4.0, 3)
+    dirs_cam = scenes.pixel_directions(800, 800, 960.0, device).reshape(-1, 3)
+    g = torch.Generator(device=device).manual_seed(seed)
+    gc = torch.Generator().manual_seed(seed)
+    out = []
+    m8 = scene.mask.view(torch.uint8)
+    while len(out) < count:
+        c2w = cams[int(torch.randint(0, 100, (1,), generator=gc))].to(device)
+        pick = torch.randint(0, dirs_cam.shape[0], (3 * BATCH,), generator=g, device=device)
+        d = dirs_cam[pick] @ c2w[:, :3].t()
+        d = (d / d.norm(dim=-1, keepdim=True)).contiguous()
+        o = c2w[:, 3].expand(d.shape).contiguous()
+        num = torch.empty(d.shape[0], dtype=torch.int32, device=device)
+        N.call("dv_masked_count", d.shape[0], scene.xyzmin, float(scene.voxel_num), scene.voxel_size, 1.0,
+               N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, N.stream(device))
+        keep = torch.nonzero(num > 0)[:, 0]
+        if keep.numel() < BATCH:
+            continue
+        keep = keep[:BATCH]
+        tgt = torch.rand(BATCH, 3, generator=g, device=device)
+        out.append((o[keep].contiguous(), d[keep].contiguous(), tgt))
+    return out
+
+
+def train_step(field, o, d, tgt):
+    import torch
+
+    rgb, reg = field(o, d)
+    loss = torch.nn.functional.mse_loss(rgb, tgt) + L_S * reg
+    gv, gp = torch.autograd.grad(loss, [field.voxels, field.params])
+    return loss, gv, gp
+
+
+def frame_rays(scene, k, device):
+    from diver_gb300 import scenes
+
+    cams = scenes.sphere_cameras(100, 4.0, 3)
+    return scenes.camera_rays(cams[k % 100], 800, 800, 960.0, device)
+
+
+# --- our arm -------------------------------------------------------------------
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import diver_gb300.renderer as R
+    from diver_gb300.renderer import DIVeRField
+
+    dev = torch.device("cuda", local)
+    scene = train_scene(dev)
+    field = DIVeRField.from_scene(scene, dev)
+    batches = make_batches(scene, args.warmup + args.steps, dev)
+    # warm-up
+    for i in range(args.warmup):
+        train_step(field, *batches[i])
+    torch.cuda.synchronize()
+    # ---- timed: device-resident inputs ----
+    R.KERNEL_EVENTS = {}
+    barrier(world)
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        segs_total = 0
+        for i in range(args.steps):
+            o, d, tgt = batches[args.warmup + i]
+            train_step(field, o, d, tgt)
+        end.record()
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = start.elapsed_time(end)
+    kernel_ms = {k: [s.elapsed_time(e) for s, e in v] for k, v in R.KERNEL_EVENTS.items()}
+    R.KERNEL_EVENTS = None
+    # segments per step (for the roofline): recount with the same traversal
+    seg_counts = [field.segments(*batches[args.warmup + i][:2]).total for i in range(args.steps)]
+    ms_max = allreduce_max(ms, world)
+    rays = allreduce_sum(float(BATCH * args.steps), world)
+    value = rays / (ms_max * 1e-3) / 1e6
+    # ---- e2e: pinned host inputs, H2D + D2H inside the timed region ----
+    host = [tuple(t.cpu().pin_memory() for t in b) for b in batches[args.warmup:]]
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for o_h, d_h, g_h in host:
+        o, d, tgt = (x.to(dev, non_blocking=True) for x in (o_h, d_h, g_h))
+        loss, _, _ = train_step(field, o, d, tgt)
+        loss.item()
+    t1.record()
+    torch.cuda.synchronize()
+    e2e_ms = allreduce_max(t0.elapsed_time(t1), world)
+    e2e_val = rays / (e2e_ms * 1e-3) / 1e6
+    # ---- render: full frames, forward only ----
+    render = None
+    if not args.no_render:
+        times = []
+        with torch.no_grad():
+            for k in range(2 + args.frames):
+                o, d = frame_rays(scene, k, dev)
+                torch.cuda.synchronize()
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record()
+                field(o, d)
+                e.record()
+                torch.cuda.synchronize()
+                if k >= 2:
+                    times.append(s.elapsed_time(e))
+        times.sort()
+        p50 = statistics.median(times)
+        p99 = times[min(len(times) - 1, int(round(0.99 * (len(times) - 1))))]
+        render = {"form": "plain_fp32", "resolution": [800, 800], "Mrays_per_s": 640000 / (p50 * 1e-3) / 1e6,
+                  "p50_ms": p50, "p99_ms": p99, "frames": len(times)}
+    # ---- roofline of the dominant kernel ----
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    tot = {k: sum(v) for k, v in kernel_ms.items()}
+    dom = max(tot, key=tot.get)
+    avg_ms = tot[dom] / len(kernel_ms[dom])
+    flops = FLOP_PER_SEG.get(dom, 0) * statistics.mean(seg_counts)
+    peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    achieved = flops / (avg_ms * 1e-3) / 1e12 if flops else None
+    roofline = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (measured)" if peaks else "fallback",
+                "avg_launch_ms": avg_ms, "segments_per_launch": statistics.mean(seg_counts),
+                "kernel_share": {k: v / sum(tot.values()) for k, v in tot.items()}}
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded 256^3x32 grid N(0,0.02^2), 16-blob occupancy ~60%, 100 cameras 800x800, "
+                "targets U[0,1]",
+        "config": {"workload": "train fwd+bwd, DIVeR32, 256^3 x 32 features, batch 4096 rays that hit occupied voxels",
+                   "global_batch": BATCH * world, "form": "plain_fp32", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (2.2 GB grid), a fresh batch every step"},
+        "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": BATCH * 9 * 4, "d2h_bytes_per_step": 4},
+        "gpu_launches": OUR_LAUNCHES_PER_STEP * args.steps,
+        "roofline": roofline,
+        "render": render,
+        "segments_per_step": statistics.mean(seg_counts),
+    }
+    line["clocks"] = clk.summary()
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(scene, batches[args.warmup], sample=256, repeats=3)
+    return line
+
+
+# --- CPU reference path (oracle port) ------------------------------------------
+
+def cpu_sample_step(feat_cpu, mask_np, scene, layers, o, d, tgt):
+    import numpy as np
+    import torch
+
+    from oracle import native as orc
+    from oracle import torch_ref
+
+    inter, num, _ = orc.masked_walk(o, d, scene.xyzmin, scene.voxel_num, scene.voxel_size, mask_np, 1.0)
+    seg = torch.from_numpy(orc.csr_from_padded(inter, num))
+    ray = torch.from_numpy(np.repeat(np.arange(len(num)), num))
+    V = feat_cpu.requires_grad_(True)
+    L = [(w.requires_grad_(True), b.requires_grad_(True)) for w, b in layers]
+    rgb, sigma, _ = torch_ref.forward(V, L, 3, seg, ray, torch.from_numpy(num), torch.from_numpy(d))
+    loss = torch_ref.loss(rgb, torch.from_numpy(tgt), sigma)
+    loss.backward()
+    V.grad = None
+    return loss.item()
+
+
+def cpu_baseline(scene, batch, sample=256, repeats=3):
+    import torch
+
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    feat = scene.features.detach().cpu()
+    mask_np = scene.mask.cpu().numpy()
+    layers = [(w.detach().cpu().clone(), b.detach().cpu().clone()) for w, b in scene.decoder.layers]
+    o, d, tgt = (x[:sample].cpu().numpy() for x in batch)
+    cpu_sample_step(feat, mask_np, scene, layers, o, d, tgt)
+    ts = []
+    for _ in range(repeats):
+        t = time.perf_counter()
+        cpu_sample_step(feat, mask_np, scene, layers, o, d, tgt)
+        ts.append(time.perf_counter() - t)
+    sec = statistics.median(ts)
+    return {"value": sample / sec / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+            "sample": f"{sample} rays of one training batch, fwd+bwd (C traversal + torch CPU integrate/decoder/render/"
+                      f"loss/autograd), median of {repeats}"}
+
+
+def run_reference(args, rank, world):
+    import torch
+
+    if rank != 0:
+        return None
+    dev = torch.device("cuda", 0) if torch.cuda.is_available() else torch.device("cpu")
+    scene = train_scene(dev)
+    batches = make_batches(scene, 1, dev) if dev.type == "cuda" else None
+    feat = scene.features.detach().cpu()
+    mask_np = scene.mask.cpu().numpy()
+    layers = [(w.detach().cpu().clone(), b.detach().cpu().clone()) for w, b in scene.decoder.layers]
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    sample = 256
+    o, d, tgt = (x.cpu().numpy() for x in batches[0])
+    for i in range(args.warmup):
+        cpu_sample_step(feat, mask_np, scene, layers, o[:sample], d[:sample], tgt[:sample])
+    t = time.perf_counter()
+    for i in range(args.steps):
+        j = (i * sample) % (BATCH - sample)
+        cpu_sample_step(feat, mask_np, scene, layers, o[j:j + sample], d[j:j + sample], tgt[j:j + sample])
+    sec = time.perf_counter() - t
+    value = sample * args.steps / sec / 1e6
+    return {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "impl": "reference",
+        "data": "synthetic: same scene and batches as the GPU arm",
+        "config": {"workload": "train fwd+bwd, DIVeR32, 256^3 x 32 features, batch 4096 rays that hit occupied voxels",
+                   "global_batch": BATCH, "form": "reference algorithm on host cores", "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} rays per step of the training workload (C traversal restatement + "
+                                   f"torch CPU integrate/decoder/render/loss/autograd)"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -35,6 +35,12 @@ SIGNATURES = {
     "dv_exclusive_scan": (I32, [P, I64, P, P, P]),
     "dv_integrate_fwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_integrate_bwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
+    "dv_decoder_param_count": (I32, [I32, I32]),
+    "dv_ray_pe": (I32, [I32, I32, P, I32, P, P, P, P]),
+    "dv_decode_fwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P]),
+    "dv_composite_fwd": (I32, [I32, P, P, I32, P, P, P, P]),
+    "dv_composite_bwd": (I32, [I32, P, P, P, P, F32, P, P]),
+    "dv_decode_bwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, P, P]),
     "dv_aabb_intersect": (I32, [I32, P, P, P, P, P, P, I32, P]),
     "dv_ray_march": (I32, [I32, P, P, P, P, I32, P]),
 }

@@ -123,10 +123,11 @@ class Segments:
     t [S] float32 distances, ray [S] int32 ray index, counts [B] int32.
     """
 
-    __slots__ = ("offsets", "seg", "t", "ray", "counts")
+    __slots__ = ("offsets", "seg", "t", "ray", "counts", "max_count")
 
-    def __init__(self, offsets, seg, t, ray, counts):
+    def __init__(self, offsets, seg, t, ray, counts, max_count=None):
         self.offsets, self.seg, self.t, self.ray, self.counts = offsets, seg, t, ray, counts
+        self.max_count = int(counts.max()) if max_count is None and counts.numel() else (max_count or 0)
 
     @property
     def coord_in(self) -> torch.Tensor:
@@ -141,6 +142,14 @@ class Segments:
         return self.seg.shape[0]
 
 
+def _totals(offsets: torch.Tensor, counts: torch.Tensor) -> tuple[int, int]:
+    """(total segments, max per ray) with a single device-to-host read."""
+    if counts.numel() == 0:
+        return 0, 0
+    S, M = torch.stack([offsets[-1], counts.max().to(torch.int64)]).tolist()
+    return int(S), int(M)
+
+
 def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale) -> Segments:
     """Segments of occupied voxels; equals coord[mask] of masked_intersect's output
     (model/diver.py:86-93), t = exit distance."""
@@ -152,14 +161,14 @@ def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale) -> Se
     N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
            N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), None, st)
     offsets = exclusive_scan(num)
-    S = int(offsets[-1].item())
+    S, M = _totals(offsets, num)
     seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
     t = torch.empty(S, dtype=torch.float32, device=dev)
     ray = torch.empty(S, dtype=torch.int32, device=dev)
     if S > 0:
         N.call("dv_masked_segments", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
                N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
-    return Segments(offsets, seg, t, ray, num)
+    return Segments(offsets, seg, t, ray, num, M)
 
 
 def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
@@ -174,11 +183,11 @@ def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
     pairs = torch.empty_like(num)
     N.call("dv_dense_pair_counts", B, N.ptr(num), N.ptr(pairs), st)
     offsets = exclusive_scan(pairs)
-    S = int(offsets[-1].item())
+    S, M = _totals(offsets, pairs)
     seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
     t = torch.empty(S, dtype=torch.float32, device=dev)
     ray = torch.empty(S, dtype=torch.int32, device=dev)
     if S > 0:
         N.call("dv_dense_segments", B, float(xyzmin), float(voxel_num), float(voxel_size),
                N.ptr(o), N.ptr(v), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
-    return Segments(offsets, seg, t, ray, pairs)
+    return Segments(offsets, seg, t, ray, pairs, M)

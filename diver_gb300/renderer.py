@@ -1,0 +1,145 @@
+"""Training / offline render path: traversal -> integral -> decoder -> compositing.
+
+`render_segments` is a torch.autograd.Function over the CUDA pipeline:
+  forward   dv_ray_pe, dv_decode_fwd, dv_composite_fwd
+  backward  dv_composite_bwd, dv_decode_bwd (recomputes each segment's decode
+            instead of storing activations; grid gradient by vector atomics)
+It returns per-ray rgb and the reference's sparsity term
+mean(log(1 + sigma^2 / 0.5)) over the padded [B, M] sigma (train.py:84-85),
+so `mse(rgb, target) + l_s * reg` is the reference's training loss
+(train.py:109-113) and autograd delivers gradients for the feature grid and
+the packed decoder parameters.
+
+`DIVeRField` bundles a scene's grid, occupancy mask and decoder the way the
+reference's DIVeR module does (model/diver.py:16-207) for callers that want a
+module.
+"""
+from __future__ import annotations
+
+import torch
+from torch.autograd import Function
+
+from . import _native as N
+from .decoder import Decoder, pack_plain
+from .ray_voxel_intersection import Segments, dense_segments, masked_segments
+
+KIND_ID = {"diver32": 32, "diver64": 64}
+WIDTH = {32: 32, 64: 64}
+
+# Optional per-kernel timing: when set to a dict, the pipeline records a CUDA
+# event pair (on the launching stream) around each decoder / compositing launch,
+# keyed by entry-point name.
+KERNEL_EVENTS: dict | None = None
+
+
+def _timed(name: str, *args) -> None:
+    if KERNEL_EVENTS is None:
+        N.call(name, *args)
+        return
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    N.call(name, *args)
+    e.record()
+    KERNEL_EVENTS.setdefault(name, []).append((s, e))
+
+
+def _grid(voxels: torch.Tensor):
+    N.need_cuda("voxels", voxels, torch.float32)
+    if voxels.dim() != 4 or voxels.shape[-1] not in (32, 64):
+        raise ValueError(f"voxels must be [Nz, Ny, Nx, 32|64], got {tuple(voxels.shape)}")
+    nz, ny, nx, c = voxels.shape
+    return nx, ny, nz, c
+
+
+def _check_params(kind: int, channels: int, params: torch.Tensor):
+    n = N.lib().dv_decoder_param_count(kind, channels)
+    if n <= 0:
+        raise ValueError(f"unsupported decoder kind {kind} with {channels} channels")
+    N.need_cuda("params", params, torch.float32)
+    if params.numel() != n:
+        raise ValueError(f"packed decoder must hold {n} floats, got {params.numel()}")
+
+
+class SegmentRender(Function):
+    @staticmethod
+    def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool):
+        nx, ny, nz, c = _grid(voxels)
+        _check_params(kind, c, params)
+        N.need_cuda("dirs", dirs, torch.float32)
+        B = dirs.shape[0]
+        dev = voxels.device
+        st = N.stream(dev)
+        W = WIDTH[kind]
+        pe_feat = torch.empty(B, 28, device=dev)
+        pe_out = torch.empty(B, W, device=dev)
+        _timed("dv_ray_pe", kind, c, N.ptr(params), B, N.ptr(dirs), N.ptr(pe_feat), N.ptr(pe_out), st)
+        S = seg.total
+        out4 = torch.empty(S, 4, device=dev)
+        _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), S,
+               N.ptr(pe_out), N.ptr(out4), st)
+        rgb = torch.empty(B, 3, device=dev)
+        reg = torch.empty(B, device=dev)
+        _timed("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), int(bool(white_back)), N.ptr(rgb), None,
+               N.ptr(reg), st)
+        M = max(seg.max_count, 1)
+        reg_mean = reg.sum() / float(B * M)
+        ctx.save_for_backward(voxels, params, dirs, pe_feat, pe_out, out4, rgb)
+        ctx.seg, ctx.kind, ctx.BM = seg, kind, float(B * M)
+        return rgb, reg_mean
+
+    @staticmethod
+    def backward(ctx, g_rgb, g_reg):
+        voxels, params, dirs, pe_feat, pe_out, out4, rgb = ctx.saved_tensors
+        seg = ctx.seg
+        nx, ny, nz, c = _grid(voxels)
+        dev = voxels.device
+        st = N.stream(dev)
+        B = dirs.shape[0]
+        g_rgb = (g_rgb if g_rgb is not None else torch.zeros(B, 3, device=dev)).contiguous()
+        reg_coef = float(g_reg) / ctx.BM if g_reg is not None else 0.0
+        d4 = torch.empty_like(out4)
+        _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb), reg_coef, N.ptr(d4), st)
+        gv = torch.zeros_like(voxels)
+        gp = torch.zeros_like(params)
+        _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
+               seg.total, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
+        return gv, gp, None, None, None, None
+
+
+def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True):
+    """(rgb [B,3], sparsity term) for the CSR segments of B rays."""
+    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back)
+
+
+class DIVeRField(torch.nn.Module):
+    """Explicit-grid DIVeR on the CUDA path: voxels [N+1]^3 x C and a packed
+    decoder as parameters, an occupancy mask as a buffer."""
+
+    def __init__(self, voxels: torch.Tensor, decoder: Decoder, mask: torch.Tensor | None, xyzmin: float,
+                 voxel_size: float, mask_scale: float = 1.0, white_back: bool = True):
+        super().__init__()
+        self.voxels = torch.nn.Parameter(voxels.contiguous())
+        self.params = torch.nn.Parameter(pack_plain(decoder).to(voxels.device))
+        self.register_buffer("voxel_mask", None if mask is None else mask.contiguous())
+        self.kind = decoder.kind
+        self.voxel_num = voxels.shape[0] - 1
+        self.xyzmin = float(xyzmin)
+        self.voxel_size = float(voxel_size)
+        self.mask_scale = float(mask_scale)
+        self.white_back = white_back
+
+    @staticmethod
+    def from_scene(scene, device="cuda") -> "DIVeRField":
+        return DIVeRField(scene.features.to(device), scene.decoder, scene.mask.to(device), scene.xyzmin,
+                          scene.voxel_size, scene.mask_scale, scene.white_back)
+
+    def segments(self, os: torch.Tensor, ds: torch.Tensor) -> Segments:
+        if self.voxel_mask is not None:
+            return masked_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, self.voxel_mask,
+                                   self.mask_scale)
+        return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size)
+
+    def forward(self, os: torch.Tensor, ds: torch.Tensor):
+        """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207)."""
+        seg = self.segments(os.contiguous(), ds.contiguous())
+        return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back)

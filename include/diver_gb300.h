@@ -159,6 +159,48 @@ DV_API int dv_integrate_bwd(const float* grad_feature, int nvx, int nvy, int nvz
                             long long n_seg, float* grad_voxels, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Decoder + compositing, training/offline path (plain FP32).
+ *
+ * kind 32 = DIVeR32 (mlp_point [32,2,33], mlp_view [32,1]),
+ * kind 64 = DIVeR64 (mlp_point [64,1,65], mlp_view [64,1]); channels 32|64.
+ * params: the packed torch form, every nn.Linear of mlp1 then mlp2 as
+ * W^T [in][out4] (out4 = out rounded up to 4, extra columns 0) followed by the
+ * bias [out4]; dv_decoder_param_count gives its length in floats.
+ * Segments are the CSR lists of dv_masked_segments / dv_dense_segments.
+ * Replaces DIVeR.forward/decode/render (model/diver.py:159-207) and the
+ * training loss (train.py:84-85,109-113).
+ * ------------------------------------------------------------------------ */
+
+DV_API int dv_decoder_param_count(int kind, int channels);
+
+/* Per-ray positional encoding pe_feat [batch][28] (27 used) and its
+ * contribution to mlp2's first layer incl. bias, pe_out [batch][width]. */
+DV_API int dv_ray_pe(int kind, int channels, const float* params, int batch, const float* dirs,
+                     float* pe_feat, float* pe_out, void* stream);
+
+/* out4 [n_seg][4] = (sigma_raw, sigmoid rgb) per segment. */
+DV_API int dv_decode_fwd(int kind, int channels, const float* params, const float* voxels, int nvx,
+                         int nvy, int nvz, const float* seg, const int* seg_ray, long long n_seg,
+                         const float* pe_out, float* out4, void* stream);
+
+/* rgb [batch][3] (+ T_final if white_back), optional t_final [batch] and
+ * reg_sum [batch] = sum over the ray's segments of log(1 + sigma^2 / 0.5). */
+DV_API int dv_composite_fwd(int batch, const int64_t* offsets, const float* out4, int white_back,
+                            float* rgb, float* t_final, float* reg_sum, void* stream);
+
+/* d4 [n_seg][4] = (dL/dsigma_raw, dL/drgb_seg) from grad_rgb [batch][3];
+ * reg_coef multiplies d/dsigma log(1 + sigma^2/0.5). */
+DV_API int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4, const float* rgb,
+                            const float* grad_rgb, float reg_coef, float* d4, void* stream);
+
+/* Accumulates the feature-grid gradient (grad_voxels, same layout as voxels)
+ * and the packed parameter gradient (grad_params) of the segments' decode. */
+DV_API int dv_decode_bwd(int kind, int channels, const float* params, const float* voxels, int nvx,
+                         int nvy, int nvz, const float* seg, const int* seg_ray, long long n_seg,
+                         const float* pe_feat, const float* pe_out, const float* d4,
+                         float* grad_voxels, float* grad_params, void* stream);
+
+/* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.
  * ------------------------------------------------------------------------ */
 
