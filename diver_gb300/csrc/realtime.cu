@@ -1,0 +1,236 @@
+// Real-time fused decoder: per pixel, up to 8 recorded hits per call, the
+// closed-form integral of the sparse feature table, the folded MLP, and
+// front-to-back compositing with the reference's skip (alpha < 1e-2) and
+// early-termination (T < 1e-2) rules.
+// Reference: utils/mlp_evaluation/src/mlp_eval.cu:32-231 (DIVeR32) and
+// utils/mlp_evaluation64/src/mlp_eval.cu:32-231 (DIVeR64).
+//
+// Differences from the reference, by design: no process-global state (the
+// reference binds a 3D texture and a __constant__ array in upload_weight);
+// the voxel index map and the weights are per-model device buffers passed to
+// every call, so several models can be resident.  The clamped texture lookup
+// becomes an explicit clamp.  The weights are re-laid out once at upload
+// (dv_realtime_pack) so every row is float4 aligned and they are staged in
+// shared memory.  Math uses expf/sincosf, not the fast intrinsics.
+#include "common.cuh"
+#include "integrate.cuh"
+#include "mlp.cuh"
+
+namespace dv {
+
+// Aligned real-time layout (floats), width W, FIRST = 1 for DIVeR32 (bias of
+// the pre-multiplied first layer, applied to the integrated feature):
+//   [FIRST] b_in [32]
+//   L0   bias [W], W^T [32][W]       (weight0: 32 -> W)
+//   SIG  w [W], bias, pad -> W+4     (weight1: sigma)
+//   L2   bias [W], W^T [W][W], W^T_pe [28][W] (torch PE order, row 27 zero)
+//   L3   bias [4], W^T [W][4]        (weight3: W -> 3)
+template <int W, int FIRST>
+struct RtLayout {
+  static constexpr int b_in = 0;
+  static constexpr int l0_b = FIRST ? 32 : 0;
+  static constexpr int l0_w = l0_b + W;
+  static constexpr int sig = l0_w + 32 * W;
+  static constexpr int l2_b = sig + W + 4;
+  static constexpr int l2_w = l2_b + W;
+  static constexpr int l2_pe = l2_w + W * W;
+  static constexpr int l3_b = l2_pe + PE_PAD * W;
+  static constexpr int l3_w = l3_b + 4;
+  static constexpr int size = l3_w + W * 4;
+};
+
+// Reference params index of the PE weight of torch PE column k (the reference
+// stores per axis [d, sin x4, cos x4]; convert.py:89-92,128-131).
+__host__ __device__ inline int pe_ref_row(int k) {
+  if (k < 3) return k * 9;
+  const int band = (k - 3) / 6, r = (k - 3) % 6, ax = r % 3;
+  return ax * 9 + (r < 3 ? 1 + band : 5 + band);
+}
+
+template <int W, int FIRST>
+__global__ void pack_kernel(const float* __restrict__ ref, float* __restrict__ out) {
+  using L = RtLayout<W, FIRST>;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= L::size) return;
+  // reference offsets (convert.py:94-140)
+  const int r0 = FIRST ? 32 : 0;      // weight0^T [33][W]: bias row then 32 rows
+  const int r1 = r0 + 33 * W;         // weight1 [W+1]: sigma bias, weights
+  const int r2 = r1 + W + 1;          // w2^T [1+W+27][W]
+  const int r3 = r2 + (1 + W + 27) * W;  // weight3^T [W+1][3]
+  float v = 0.f;
+  int i = tid;
+  if (FIRST && i < 32) {
+    v = ref[i];
+  } else if (i >= L::l0_b && i < L::l0_w) {
+    v = ref[r0 + (i - L::l0_b)];
+  } else if (i >= L::l0_w && i < L::sig) {
+    v = ref[r0 + W + (i - L::l0_w)];
+  } else if (i >= L::sig && i < L::sig + W) {
+    v = ref[r1 + 1 + (i - L::sig)];
+  } else if (i == L::sig + W) {
+    v = ref[r1];
+  } else if (i >= L::l2_b && i < L::l2_w) {
+    v = ref[r2 + (i - L::l2_b)];
+  } else if (i >= L::l2_w && i < L::l2_pe) {
+    v = ref[r2 + W + (i - L::l2_w)];
+  } else if (i >= L::l2_pe && i < L::l3_b) {
+    const int k = (i - L::l2_pe) / W, j = (i - L::l2_pe) % W;
+    v = k < PE_DIM ? ref[r2 + (1 + W + pe_ref_row(k)) * W + j] : 0.f;
+  } else if (i >= L::l3_b && i < L::l3_b + 3) {
+    v = ref[r3 + (i - L::l3_b)];
+  } else if (i >= L::l3_w) {
+    const int row = (i - L::l3_w) / 4, j = (i - L::l3_w) % 4;
+    v = j < 3 ? ref[r3 + 3 * (1 + row) + j] : 0.f;
+  }
+  out[tid] = v;
+}
+
+struct RtArgs {
+  int batch;
+  const float* coords;   // [8][B][6]
+  const float* feats;    // [F][32]
+  const int* vmap;       // [(N+1)^3]
+  int ms;                // N+1
+  const float* params;   // aligned layout
+  const float* v;        // [B][3]
+  float* rgba;           // [B][4]
+  uint8_t* finish;       // [B]
+};
+
+__device__ __forceinline__ int clampi(int x, int hi) { return x < 0 ? 0 : (x > hi ? hi : x); }
+
+template <int W, int FIRST>
+__global__ void __launch_bounds__(128) mlp_eval_kernel(const RtArgs a) {
+  using L = RtLayout<W, FIRST>;
+  extern __shared__ __align__(16) float smem[];
+  float* sw = smem;
+  float* rows = smem + L::size;
+  for (int i = threadIdx.x; i < L::size / 4; i += blockDim.x)
+    reinterpret_cast<float4*>(sw)[i] = __ldg(reinterpret_cast<const float4*>(a.params) + i);
+  __syncthreads();
+  float* X = rows + threadIdx.x * (W + 4);               // integrated feature / h2
+  float* H = rows + (blockDim.x + threadIdx.x) * (W + 4);  // h1
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.batch || a.finish[b]) return;
+  float pe[PE_PAD];
+  pos_enc(__ldg(a.v + 3 * b), __ldg(a.v + 3 * b + 1), __ldg(a.v + 3 * b + 2), pe);
+  float4 acc = reinterpret_cast<float4*>(a.rgba)[b];
+  const long long stride = (long long)a.batch * 6;
+  float y[W + 4];
+  for (int hit = 0; hit < 8; ++hit) {
+    const float* c = a.coords + hit * stride + (long long)b * 6;
+    const float x0 = c[0], y0 = c[1], z0 = c[2], x1 = c[3], y1 = c[4], z1 = c[5];
+    if (x0 < 0.f) {
+      a.finish[b] = 1;
+      break;
+    }
+    // corner weights; the index clamp of segment_corners is replaced by the
+    // texture-style clamp of each lookup (mlp_eval.cu:112-118)
+    const SegCorner sc = segment_corners(x0, y0, z0, x1, y1, z1, 1 << 30, 1 << 30, 1 << 30);
+    float f[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) f[k] = FIRST ? sw[L::b_in + k] : 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int x = clampi(sc.x + (j & 1), a.ms - 1);
+      const int yy = clampi(sc.y + ((j >> 1) & 1), a.ms - 1);
+      const int z = clampi(sc.z + (j >> 2), a.ms - 1);
+      const int idx = __ldg(a.vmap + ((long long)z * a.ms + yy) * a.ms + x);
+      const float4* row = reinterpret_cast<const float4*>(a.feats + (long long)idx * 32);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 v = __ldg(row + q);
+        f[4 * q] = fmaf(sc.w[j], v.x, f[4 * q]);
+        f[4 * q + 1] = fmaf(sc.w[j], v.y, f[4 * q + 1]);
+        f[4 * q + 2] = fmaf(sc.w[j], v.z, f[4 * q + 2]);
+        f[4 * q + 3] = fmaf(sc.w[j], v.w, f[4 * q + 3]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 32; ++k) X[k] = FIRST ? fmaxf(f[k], 0.f) : f[k];
+    dense_fwd_s<W, false>(sw + L::l0_w, sw + L::l0_b, X, 32, y);
+#pragma unroll
+    for (int k = 0; k < W; ++k) H[k] = fmaxf(y[k], 0.f);
+    float sigma = sw[L::sig + W];
+#pragma unroll 8
+    for (int k = 0; k < W; ++k) sigma = fmaf(sw[L::sig + k], H[k], sigma);
+    const float alpha = 1.f - expf(-fmaxf(sigma, 0.f));
+    if (alpha < 1e-2f) continue;
+    dense_fwd_s<W, false>(sw + L::l2_w, sw + L::l2_b, H, W, y);
+#pragma unroll
+    for (int k = 0; k < PE_DIM; ++k) {
+      const float p = pe[k];
+#pragma unroll
+      for (int j = 0; j < W; j += 4) {
+        const float4 w = *reinterpret_cast<const float4*>(sw + L::l2_pe + k * W + j);
+        y[j] = fmaf(p, w.x, y[j]);
+        y[j + 1] = fmaf(p, w.y, y[j + 1]);
+        y[j + 2] = fmaf(p, w.z, y[j + 2]);
+        y[j + 3] = fmaf(p, w.w, y[j + 3]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < W; ++k) X[k] = fmaxf(y[k], 0.f);
+    float o[4];
+    dense_fwd_s<4, false>(sw + L::l3_w, sw + L::l3_b, X, W, o);
+    const float wgt = acc.w * alpha;
+    acc.x += wgt * sigmoidf_acc(o[0]);
+    acc.y += wgt * sigmoidf_acc(o[1]);
+    acc.z += wgt * sigmoidf_acc(o[2]);
+    acc.w = acc.w * (1.f - alpha);
+    if (acc.w < 1e-2f) {
+      a.finish[b] = 1;
+      break;
+    }
+  }
+  reinterpret_cast<float4*>(a.rgba)[b] = acc;
+}
+
+template <int W, int FIRST>
+int launch_mlp_eval(const RtArgs& a, cudaStream_t st) {
+  using L = RtLayout<W, FIRST>;
+  const size_t smem = (size_t)(L::size + 2 * 128 * (W + 4)) * sizeof(float);
+  auto k = mlp_eval_kernel<W, FIRST>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
+  k<<<ceil_div(a.batch, 128), 128, smem, st>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+}  // namespace dv
+
+using namespace dv;
+
+extern "C" {
+
+int dv_realtime_packed_size(int width) {
+  if (width == 32) return RtLayout<32, 1>::size;
+  if (width == 64) return RtLayout<64, 0>::size;
+  return -1;
+}
+
+int dv_realtime_pack(int width, const float* ref_params, float* packed, void* stream) {
+  DV_CHECK((width == 32 || width == 64) && ref_params && packed, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)packed & 15) == 0, DV_ERR_ARG);
+  const int n = dv_realtime_packed_size(width);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (width == 32) pack_kernel<32, 1><<<ceil_div(n, 256), 256, 0, st>>>(ref_params, packed);
+  else pack_kernel<64, 0><<<ceil_div(n, 256), 256, 0, st>>>(ref_params, packed);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_mlp_eval(int width, int batch_size, const float* coords, const float* voxels, const int* voxel_map,
+                int map_size, const float* packed_params, const float* v, float* rgba, uint8_t* finish,
+                void* stream) {
+  DV_CHECK((width == 32 || width == 64) && batch_size >= 0 && map_size > 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(coords && voxels && voxel_map && packed_params && v && rgba && finish, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)voxels & 15) == 0 && ((uintptr_t)rgba & 15) == 0 && ((uintptr_t)packed_params & 15) == 0,
+           DV_ERR_ARG);
+  RtArgs a{batch_size, coords, voxels, voxel_map, map_size, packed_params, v, rgba, finish};
+  cudaStream_t st = (cudaStream_t)stream;
+  return width == 32 ? launch_mlp_eval<32, 1>(a, st) : launch_mlp_eval<64, 0>(a, st);
+}
+
+}  // extern "C"

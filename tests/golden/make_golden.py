@@ -118,6 +118,9 @@ def make_decode(ref_root: Path, out: Path):
         with torch.no_grad():
             model.voxels.copy_(vox)
             model.voxel_mask.copy_(mask)
+            # a positive density bias so both the density and the colour
+            # branches carry gradient (default init can leave sigma <= 0)
+            model.mlp1[-1].bias[0] += 0.6
         color, sigma, m, ts = model(torch.from_numpy(o_h), torch.from_numpy(d_h))
         rgb, weight = model.render(color, sigma, m)
         loss_c = torch.nn.functional.mse_loss(rgb, torch.from_numpy(target))

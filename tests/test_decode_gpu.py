@@ -126,9 +126,16 @@ def test_gradients_match_fp64_central_differences(g, kind):
     tgt = torch.from_numpy(g["target"]).double()
     n1 = KINDS[kind]
 
-    def loss_fn(V_, L_):
+    def parts(V_, L_):
         rgb, sigma, _ = torch_ref.forward(V_, L_, n1, segs, ray, counts, dirs)
-        return torch_ref.loss(rgb, tgt, sigma).item()
+        mse = torch.nn.functional.mse_loss(rgb, tgt).item()
+        reg = torch.log(1 + sigma ** 2 / 0.5).mean().item()
+        return np.array([mse, 1e-5 * reg])
+
+    def central(Vp, Lp, Vm, Lm):
+        # difference each loss term on its own: the tiny sparsity term would
+        # otherwise be lost in the rounding of the much larger MSE
+        return float(((parts(Vp, Lp) - parts(Vm, Lm)) / (2 * h)).sum())
 
     h = 1e-6
     gen = torch.Generator().manual_seed(11)
@@ -139,7 +146,7 @@ def test_gradients_match_fp64_central_differences(g, kind):
         Vp, Vm = V.clone(), V.clone()
         Vp.view(-1)[idx] += h
         Vm.view(-1)[idx] -= h
-        fd.append((loss_fn(Vp, L) - loss_fn(Vm, L)) / (2 * h))
+        fd.append(central(Vp, L, Vm, L))
         got.append(flat[idx].item())
     for li in range(len(L)):
         w, b = L[li]
@@ -151,7 +158,7 @@ def test_gradients_match_fp64_central_differences(g, kind):
             Lm = [(x.clone(), y.clone()) for x, y in L]
             Lp[li][0][i, j] += h
             Lm[li][0][i, j] -= h
-            fd.append((loss_fn(V, Lp) - loss_fn(V, Lm)) / (2 * h))
+            fd.append(central(V, Lp, V, Lm))
             got.append(dw[i, j].item())
     got, fd = np.array(got), np.array(fd)
     rel = np.linalg.norm(got - fd) / np.linalg.norm(fd)
