@@ -1,0 +1,304 @@
+// Tensor-core (tcgen05) decoder forward for the training / offline path.
+//
+// One CTA = 128 threads = one tile of 128 segments = the 128 TMEM lanes of
+// an M=128 MMA.  Per tile:
+//   gather  C/4 threads per segment read the 8 corner rows (coalesced float4),
+//           integrate in FP32 and write the feature row as BF16/FP16 straight
+//           into the K-major A operand tile in shared memory
+//   layers  each Linear layer is one chain of K/16 tcgen05.mma (A and B from
+//           shared memory, FP32 accumulators in TMEM), committed to an
+//           mbarrier; thread t then reads its row (TMEM lane t), adds the bias,
+//           applies ReLU and writes the next A tile row
+//   output  sigma (FP32) and sigmoid(rgb) per segment
+// The decoder's weights (all layers, B operands in the same K-major layout)
+// and biases stay in shared memory for the CTA's lifetime; the grid is
+// persistent over tiles and sized so TMEM never oversubscribes.
+// Reference semantics: model/diver.py:159-180 (mlp1, PE, mlp2, sigmoid).
+#include "common.cuh"
+#include "integrate.cuh"
+#include "mlp.cuh"
+#include "tc.cuh"
+
+#include <algorithm>
+
+namespace dv {
+
+constexpr int TC_MAX_LAYERS = 5;
+
+struct TcLayer {
+  int b_off;     // byte offset of the layer's B image in the weight blob
+  int K, N;      // padded: K % 16 == 0, N % 16 == 0
+  int bias_off;  // float offset of the layer's bias (N entries)
+};
+
+struct TcArgs {
+  const float* grid;
+  int nvx, nvy, nvz;
+  const float* seg;
+  const int* seg_ray;
+  long long S;
+  const float* pe_out;  // [B][W]: bias + PE part of mlp2's first layer (FP32)
+  float4* out4;
+  const uint8_t* wblob;
+  int wbytes;  // multiple of 16
+  const float* bias;
+  int nbias;   // multiple of 4
+  TcLayer L[TC_MAX_LAYERS];
+  int* err;    // set to 1 if an MMA completion wait timed out
+};
+
+template <int C, int BF16>
+__device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long s0, uint8_t* sA) {
+  constexpr int TPS = C / 4;
+  constexpr int SPP = 128 / TPS;
+  const int t = threadIdx.x;
+#pragma unroll 1
+  for (int p = 0; p < TPS; ++p) {
+    const int ls = p * SPP + t / TPS;
+    const int q = t % TPS;
+    const long long s = s0 + ls;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (s < a.S) {
+      const float* sg = a.seg + s * 6;
+      const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
+                                           __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
+      f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
+    }
+    uint2 v = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
+    *reinterpret_cast<uint2*>(sA + tc::kmajor_offset(ls, 4 * q, C)) = v;
+  }
+}
+
+// Issues one layer's MMA chain (thread 0) and waits for it (all threads).
+template <int BF16>
+__device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, const uint8_t* sA, uint32_t tmem,
+                                         uint64_t* bar, uint32_t& phase) {
+  if (threadIdx.x == 0) {
+    tc::fence_after_sync();
+    const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
+    const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB + L.b_off);
+    const uint32_t sbo = (uint32_t)(L.K / 8) * 128;
+    for (int k = 0; k < L.K / 16; ++k)
+      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
+                  k > 0 ? 1u : 0u);
+    tc::mma_commit(bar);
+  }
+  const bool done = tc::mbar_wait_bounded(bar, phase);
+  phase ^= 1u;
+  tc::fence_after_sync();
+  return done;
+}
+
+// Writes 32 values (columns c0..c0+31 of the next layer's input) of row t.
+template <int BF16>
+__device__ __forceinline__ void store_row32(uint8_t* sA, int t, int c0, int K, const float* v) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    uint4 w;
+    w.x = tc::pack2<BF16>(v[8 * j + 0], v[8 * j + 1]);
+    w.y = tc::pack2<BF16>(v[8 * j + 2], v[8 * j + 3]);
+    w.z = tc::pack2<BF16>(v[8 * j + 4], v[8 * j + 5]);
+    w.w = tc::pack2<BF16>(v[8 * j + 6], v[8 * j + 7]);
+    *reinterpret_cast<uint4*>(sA + tc::kmajor_offset(t, c0 + 8 * j, K)) = w;
+  }
+}
+
+__device__ __forceinline__ void sync_for_mma() {
+  tc::fence_before_sync();
+  tc::fence_async_smem();
+  __syncthreads();
+}
+
+// NCOLS: TMEM columns (>= widest N, power of two >= 32).
+template <int C, int W, int D1, int BF16, int NCOLS>
+__global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
+  constexpr int KMAX = C > W ? C : W;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sB = smem;
+  float* sBias = reinterpret_cast<float*>(smem + a.wbytes);
+  uint8_t* sA = reinterpret_cast<uint8_t*>(sBias + a.nbias);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sA + 128 * KMAX * 2);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int t = threadIdx.x, warp = t >> 5;
+  for (int i = t; i < a.wbytes / 16; i += 128)
+    reinterpret_cast<uint4*>(sB)[i] = __ldg(reinterpret_cast<const uint4*>(a.wblob) + i);
+  for (int i = t; i < a.nbias; i += 128) sBias[i] = __ldg(a.bias + i);
+  if (t == 0) {
+    tc::mbar_init(bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, NCOLS);
+    tc::tmem_relinquish();
+  }
+  sync_for_mma();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
+  uint32_t phase = 0;
+  bool ok = true;
+  const long long tiles = (a.S + 127) / 128;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long s0 = tile * 128;
+    const long long s = s0 + t;
+    const bool valid = s < a.S;
+    gather_tile_lp<C, BF16>(a, s0, sA);
+    sync_for_mma();
+    float v[32];
+    // mlp1 hidden layers: D = relu(A W^T + b)
+#pragma unroll 1
+    for (int l = 0; l < D1 && ok; ++l) {
+      ok = tc_layer<BF16>(a.L[l], sB, sA, tmem, bar, phase);
+      ok = __syncthreads_and(ok);
+      if (!ok) break;
+#pragma unroll
+      for (int c0 = 0; c0 < W; c0 += 32) {
+        tc::ld_32x32b_x32(trow + c0, v);
+        tc::ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + sBias[a.L[l].bias_off + c0 + i], 0.f);
+        store_row32<BF16>(sA, t, c0, W, v);
+      }
+      sync_for_mma();
+    }
+    if (!ok) break;
+    // mlp1 output: columns 0..W-1 hidden (no activation), column W sigma
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1], sB, sA, tmem, bar, phase));
+    if (!ok) break;
+    float sigma;
+    {
+      float sv[4];
+      tc::ld_32x32b_x4(trow + W, sv);
+      tc::ld_wait();
+      sigma = sv[0] + sBias[a.L[D1].bias_off + W];
+    }
+#pragma unroll
+    for (int c0 = 0; c0 < W; c0 += 32) {
+      tc::ld_32x32b_x32(trow + c0, v);
+      tc::ld_wait();
+#pragma unroll
+      for (int i = 0; i < 32; ++i) v[i] += sBias[a.L[D1].bias_off + c0 + i];
+      store_row32<BF16>(sA, t, c0, W, v);
+    }
+    sync_for_mma();
+    // mlp2 first layer: relu(hidden W^T + per-ray (bias + PE term))
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 1], sB, sA, tmem, bar, phase));
+    if (!ok) break;
+    {
+      const int ray = valid ? __ldg(a.seg_ray + s) : 0;
+      const float4* po = reinterpret_cast<const float4*>(a.pe_out + (long long)ray * W);
+#pragma unroll
+      for (int c0 = 0; c0 < W; c0 += 32) {
+        tc::ld_32x32b_x32(trow + c0, v);
+        tc::ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; i += 4) {
+          const float4 p = __ldg(po + (c0 + i) / 4);
+          v[i] = fmaxf(v[i] + p.x, 0.f);
+          v[i + 1] = fmaxf(v[i + 1] + p.y, 0.f);
+          v[i + 2] = fmaxf(v[i + 2] + p.z, 0.f);
+          v[i + 3] = fmaxf(v[i + 3] + p.w, 0.f);
+        }
+        store_row32<BF16>(sA, t, c0, W, v);
+      }
+    }
+    sync_for_mma();
+    // mlp2 output: 3 logits -> sigmoid
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 2], sB, sA, tmem, bar, phase));
+    if (!ok) break;
+    {
+      float o[4];
+      tc::ld_32x32b_x4(trow, o);
+      tc::ld_wait();
+      const int bo = a.L[D1 + 2].bias_off;
+      if (valid)
+        a.out4[s] = make_float4(sigma, sigmoidf_acc(o[0] + sBias[bo]), sigmoidf_acc(o[1] + sBias[bo + 1]),
+                                sigmoidf_acc(o[2] + sBias[bo + 2]));
+    }
+    tc::fence_before_sync();
+    __syncthreads();  // the next gather overwrites A
+  }
+  if (!ok && t == 0 && a.err) atomicExch(a.err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, NCOLS);
+}
+
+template <int C, int W, int D1, int BF16>
+int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
+  constexpr int NCOLS = W == 32 ? 64 : 128;
+  constexpr int KMAX = C > W ? C : W;
+  const size_t smem = (size_t)a.wbytes + (size_t)a.nbias * 4 + 128 * KMAX * 2 + 16;
+  auto k = decode_fwd_tc<C, W, D1, BF16, NCOLS>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  per_sm = std::min(per_sm, 512 / NCOLS);  // never oversubscribe TMEM
+  if (per_sm < 1) return DV_ERR_UNSUPPORTED;
+  const long long tiles = (a.S + 127) / 128;
+  const long long grid = std::min<long long>(tiles, (long long)sms * per_sm);
+  k<<<(unsigned)grid, 128, smem, st>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+}  // namespace dv
+
+using namespace dv;
+
+extern "C" {
+
+int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
+                     const int* layers, int n_layers, const float* voxels, int nvx, int nvy, int nvz, const float* seg,
+                     const int* seg_ray, long long n_seg, const float* pe_out, float* out4, int* err, void* stream) {
+  DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
+  const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
+  DV_CHECK(d1 > 0 && n_layers == d1 + 3 && n_layers <= TC_MAX_LAYERS, DV_ERR_ARG);
+  DV_CHECK((kind == 32 && channels == 32) || (kind == 64 && (channels == 32 || channels == 64)), DV_ERR_UNSUPPORTED);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(wblob && bias && layers && voxels && seg && seg_ray && pe_out && out4, DV_ERR_ARG);
+  DV_CHECK(wbytes > 0 && wbytes % 16 == 0 && nbias > 0 && nbias % 4 == 0, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)wblob & 15) == 0 && ((uintptr_t)voxels & 15) == 0 && ((uintptr_t)out4 & 15) == 0, DV_ERR_ARG);
+  TcArgs a{};
+  a.grid = voxels;
+  a.nvx = nvx;
+  a.nvy = nvy;
+  a.nvz = nvz;
+  a.seg = seg;
+  a.seg_ray = seg_ray;
+  a.S = n_seg;
+  a.pe_out = pe_out;
+  a.out4 = reinterpret_cast<float4*>(out4);
+  a.wblob = reinterpret_cast<const uint8_t*>(wblob);
+  a.wbytes = wbytes;
+  a.bias = bias;
+  a.nbias = nbias;
+  a.err = err;
+  const int W = kind;
+  for (int l = 0; l < n_layers; ++l) {
+    a.L[l].b_off = layers[4 * l];
+    a.L[l].K = layers[4 * l + 1];
+    a.L[l].N = layers[4 * l + 2];
+    a.L[l].bias_off = layers[4 * l + 3];
+    const TcLayer& L = a.L[l];
+    // every operand must lie inside the blob, on a 16-byte boundary, with legal MMA shapes
+    DV_CHECK(L.K % 16 == 0 && L.N % 16 == 0 && L.N >= 16 && L.N <= 256 && L.b_off % 16 == 0, DV_ERR_ARG);
+    DV_CHECK((long long)L.b_off + (long long)L.N * L.K * 2 <= wbytes && L.bias_off + L.N <= nbias, DV_ERR_ARG);
+    DV_CHECK(L.N <= (W == 32 ? 64 : 128), DV_ERR_ARG);
+  }
+  // layer shapes the kernel assumes
+  DV_CHECK(a.L[0].K == channels && a.L[0].N == W, DV_ERR_ARG);
+  for (int l = 1; l < d1; ++l) DV_CHECK(a.L[l].K == W && a.L[l].N == W, DV_ERR_ARG);
+  DV_CHECK(a.L[d1].K == W && a.L[d1].N >= W + 4, DV_ERR_ARG);
+  DV_CHECK(a.L[d1 + 1].K == W && a.L[d1 + 1].N == W && a.L[d1 + 2].K == W && a.L[d1 + 2].N >= 16, DV_ERR_ARG);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 32) return bf16 ? launch_decode_fwd_tc<32, 32, 2, 1>(a, st) : launch_decode_fwd_tc<32, 32, 2, 0>(a, st);
+  if (channels == 32)
+    return bf16 ? launch_decode_fwd_tc<32, 64, 1, 1>(a, st) : launch_decode_fwd_tc<32, 64, 1, 0>(a, st);
+  return bf16 ? launch_decode_fwd_tc<64, 64, 1, 1>(a, st) : launch_decode_fwd_tc<64, 64, 1, 0>(a, st);
+}
+
+}  // extern "C"

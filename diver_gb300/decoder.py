@@ -141,6 +141,7 @@ def unpack_plain_grad(kind: str, channels: int, flat: torch.Tensor) -> list[tupl
 PE_REORDER = [0, 3, 9, 15, 21, 6, 12, 18, 24,
               1, 4, 10, 16, 22, 7, 13, 19, 25,
               2, 5, 11, 17, 23, 8, 14, 20, 26]
+# flat params: 3168 floats for DIVeR32, 8288 for DIVeR64 over 32 channels
 REALTIME_PARAMS = {"diver32": 3168, "diver64": 8288}
 
 
@@ -171,7 +172,9 @@ def pack_realtime(dec: Decoder) -> torch.Tensor:
     w2 = torch.cat([w2[:, :-PE_DIM], w2[:, -PE_DIM:][:, PE_REORDER]], -1)
     weight3 = torch.cat([b3[:, None], w3], -1)
     params = torch.cat(head + mid + [weight1.reshape(-1), w2.t().reshape(-1), weight3.t().reshape(-1), torch.zeros(28)], 0)
-    assert params.numel() == REALTIME_PARAMS[dec.kind], params.numel()
+    expect = (32 + 33 * 32 + 33 + 60 * 32 + 33 * 3 + 28) if dec.kind == "diver32" else \
+        ((1 + dec.channels) * 64 + 65 + 92 * 64 + 65 * 3 + 28)
+    assert params.numel() == expect, params.numel()
     return params.contiguous()
 
 
@@ -182,3 +185,58 @@ def premultiply_features(dec: Decoder, features: torch.Tensor) -> torch.Tensor:
         w01 = dec.layers[0][0].to(features.device, torch.float32)
         return (features @ w01.t()).contiguous()
     return features.contiguous()
+
+
+# --- tensor-core operand image -------------------------------------------------
+
+def _kmajor_index(N: int, K: int) -> torch.Tensor:
+    """Element offsets of an [N][K] 16-bit tile in the K-major, no-swizzle
+    core-matrix layout the tcgen05 kernels read: 8x8 blocks of 128 contiguous
+    bytes, block (n/8, k/8) at ((n/8) * (K/8) + k/8) * 64 elements."""
+    n = torch.arange(N)[:, None]
+    k = torch.arange(K)[None, :]
+    return (((n // 8) * (K // 8) + k // 8) * 64 + (n % 8) * 8 + (k % 8)).reshape(-1)
+
+
+def tc_matrices(dec: Decoder):
+    """The decoder as the tensor-core kernel's layer list [(W [N][K], bias [N])]:
+    mlp1 hidden layers; mlp1's output layer with the hidden rows first and the
+    sigma row at index `width` (N padded to width + 16); the hidden-input part
+    of mlp2's first layer (its bias and PE part are added per ray in FP32);
+    mlp2's output layer (N padded to 16)."""
+    W = dec.width
+    d1 = dec.n_mlp1 - 1
+    L = [(w.detach().float().cpu(), b.detach().float().cpu()) for w, b in dec.layers]
+    mats = [L[l] for l in range(d1)]
+    w, b = L[d1]
+    wo = torch.zeros(W + 16, W)
+    bo = torch.zeros(W + 16)
+    wo[:W], wo[W] = w[1:], w[0]
+    bo[:W], bo[W] = b[1:], b[0]
+    mats.append((wo, bo))
+    w, b = L[d1 + 1]
+    mats.append((w[:, :W].clone(), torch.zeros(W)))
+    w, b = L[d1 + 2]
+    w4 = torch.zeros(16, W)
+    b4 = torch.zeros(16)
+    w4[:3], b4[:3] = w, b
+    mats.append((w4, b4))
+    return mats
+
+
+def pack_tc(dec: Decoder, bf16: bool = True):
+    """(blob uint8 [bytes], bias float32, layers int32 [n, 4] = (byte offset, K, N, bias offset))."""
+    dt = torch.bfloat16 if bf16 else torch.float16
+    images, biases, table = [], [], []
+    off = 0
+    boff = 0
+    for w, b in tc_matrices(dec):
+        N, K = w.shape
+        img = torch.zeros(N * K, dtype=dt)
+        img[_kmajor_index(N, K)] = w.reshape(-1).to(dt)
+        images.append(img.view(torch.uint8))
+        biases.append(b)
+        table.append([off, K, N, boff])
+        off += N * K * 2
+        boff += N
+    return torch.cat(images), torch.cat(biases).float(), torch.tensor(table, dtype=torch.int32)

@@ -20,7 +20,7 @@ import torch
 from torch.autograd import Function
 
 from . import _native as N
-from .decoder import Decoder, pack_plain
+from .decoder import Decoder, pack_plain, pack_tc
 from .ray_voxel_intersection import Segments, dense_segments, masked_segments
 
 KIND_ID = {"diver32": 32, "diver64": 64}
@@ -60,9 +60,27 @@ def _check_params(kind: int, channels: int, params: torch.Tensor):
         raise ValueError(f"packed decoder must hold {n} floats, got {params.numel()}")
 
 
+class TcWeights:
+    """Decoder weights in the tensor-core operand layout (BF16 or FP16) on the device."""
+
+    def __init__(self, decoder: Decoder, device, bf16: bool = True):
+        blob, bias, table = pack_tc(decoder, bf16)
+        self.blob = blob.to(device)
+        self.bias = bias.to(device)
+        self.table = table.contiguous()
+        self.bf16 = bool(bf16)
+        self.err = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def decode(self, kind, channels, voxels, seg, pe_out, out4, st):
+        nx, ny, nz, c = _grid(voxels)
+        _timed("dv_decode_fwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
+               self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), nx, ny, nz,
+               N.ptr(seg.seg), N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(out4), N.ptr(self.err), st)
+
+
 class SegmentRender(Function):
     @staticmethod
-    def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool):
+    def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None):
         nx, ny, nz, c = _grid(voxels)
         _check_params(kind, c, params)
         N.need_cuda("dirs", dirs, torch.float32)
@@ -75,8 +93,11 @@ class SegmentRender(Function):
         _timed("dv_ray_pe", kind, c, N.ptr(params), B, N.ptr(dirs), N.ptr(pe_feat), N.ptr(pe_out), st)
         S = seg.total
         out4 = torch.empty(S, 4, device=dev)
-        _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), S,
-               N.ptr(pe_out), N.ptr(out4), st)
+        if tc is None:
+            _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
+                   S, N.ptr(pe_out), N.ptr(out4), st)
+        else:
+            tc.decode(kind, c, voxels, seg, pe_out, out4, st)
         rgb = torch.empty(B, 3, device=dev)
         reg = torch.empty(B, device=dev)
         _timed("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), int(bool(white_back)), N.ptr(rgb), None,
@@ -103,12 +124,13 @@ class SegmentRender(Function):
         gp = torch.zeros_like(params)
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
-        return gv, gp, None, None, None, None
+        return gv, gp, None, None, None, None, None
 
 
-def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True):
-    """(rgb [B,3], sparsity term) for the CSR segments of B rays."""
-    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back)
+def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None):
+    """(rgb [B,3], sparsity term) for the CSR segments of B rays; `tc` selects
+    the tensor-core decoder for the forward (the backward is FP32)."""
+    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc)
 
 
 class DIVeRField(torch.nn.Module):
@@ -127,6 +149,22 @@ class DIVeRField(torch.nn.Module):
         self.voxel_size = float(voxel_size)
         self.mask_scale = float(mask_scale)
         self.white_back = white_back
+        self.decoder = decoder
+        self._tc = {}
+
+    def tc_weights(self, form: str) -> TcWeights | None:
+        """Tensor-core weights for form 'bf16' / 'fp16' (None for 'fp32'),
+        packed from the current decoder parameters."""
+        if form == "fp32":
+            return None
+        from .decoder import unpack_plain_grad
+
+        key = (form, self.params._version)
+        if key not in self._tc:
+            layers = unpack_plain_grad(self.kind, self.voxels.shape[-1], self.params.detach().cpu())
+            dec = Decoder(self.kind, self.voxels.shape[-1], layers)
+            self._tc = {key: TcWeights(dec, self.voxels.device, bf16=(form == "bf16"))}
+        return self._tc[key]
 
     @staticmethod
     def from_scene(scene, device="cuda") -> "DIVeRField":
@@ -139,7 +177,9 @@ class DIVeRField(torch.nn.Module):
                                    self.mask_scale)
         return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size)
 
-    def forward(self, os: torch.Tensor, ds: torch.Tensor):
-        """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207)."""
+    def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32"):
+        """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
+        form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder forward)."""
         seg = self.segments(os.contiguous(), ds.contiguous())
-        return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back)
+        return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back,
+                               self.tc_weights(form))

@@ -200,6 +200,21 @@ DV_API int dv_decode_bwd(int kind, int channels, const float* params, const floa
                          const float* pe_feat, const float* pe_out, const float* d4,
                          float* grad_voxels, float* grad_params, void* stream);
 
+/*
+ * Tensor-core form of dv_decode_fwd: the same decoder with its matrix
+ * products on tcgen05 (BF16 when bf16 = 1, FP16 when 0, FP32 accumulation in
+ * TMEM).  The integral, biases, PE term (pe_out, FP32), ReLU and sigmoid stay
+ * in FP32.  wblob holds every layer's weight matrix [N][K] in the K-major
+ * 8x8 core-matrix layout; `layers` is a HOST array of n_layers rows
+ * (byte offset, K, N, bias offset); bias [nbias] floats.  err (device int,
+ * optional) is set to 1 if a bounded wait for an MMA ran out.
+ */
+DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes,
+                            const float* bias, int nbias, const int* layers, int n_layers,
+                            const float* voxels, int nvx, int nvy, int nvz, const float* seg,
+                            const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
+                            int* err, void* stream);
+
 /* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.
  * ------------------------------------------------------------------------ */
@@ -231,6 +246,36 @@ DV_API int dv_aabb_intersect(int batch_size, float* coords, const float* v, cons
  */
 DV_API int dv_ray_march(int batch_size, float* coords, const float* v, const uint8_t* mask,
                  const uint8_t* finish, int voxel_num, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Real-time fused decoder (per pixel, up to 8 hits per call).
+ * ------------------------------------------------------------------------ */
+
+/* Floats of the aligned weight layout for width 32 (DIVeR32) or 64 (DIVeR64). */
+DV_API int dv_realtime_packed_size(int width);
+
+/*
+ * Re-lays out the reference's flat `params` array (convert.py:94-140; 3168
+ * floats for DIVeR32, 8288 for DIVeR64, device memory) into the aligned
+ * layout dv_mlp_eval reads.  Together with keeping the voxel map as a
+ * caller-owned device buffer this replaces upload_weight_wrapper
+ * (utils/mlp_evaluation/src/mlp_eval.cu:264-295), which binds a process-global
+ * texture and __constant__ array.
+ */
+DV_API int dv_realtime_pack(int width, const float* ref_params, float* packed, void* stream);
+
+/*
+ * One round of the real-time decoder for every unfinished pixel: up to 8 hits
+ * from coords [8][batch][6], feature table voxels [F][32], corner index map
+ * voxel_map [map_size^3] (clamped lookups), packed weights, directions v
+ * [batch][3]; updates rgba [batch][4] and finish [batch] in place.
+ * Replaces mlp_eval_wrapper + mlp_eval_kernel
+ * (utils/mlp_evaluation/src/mlp_eval.cu:32-254, width 32;
+ *  utils/mlp_evaluation64/src/mlp_eval.cu:32-254, width 64).
+ */
+DV_API int dv_mlp_eval(int width, int batch_size, const float* coords, const float* voxels,
+                       const int* voxel_map, int map_size, const float* packed_params, const float* v,
+                       float* rgba, uint8_t* finish, void* stream);
 
 #ifdef __cplusplus
 }

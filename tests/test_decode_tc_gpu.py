@@ -1,0 +1,84 @@
+"""GPU: the tcgen05 decoder (BF16 / FP16 operands, FP32 accumulation) against
+the plain FP32 decoder and the FP64 oracle.
+
+Tolerances (stated): per-segment sigma and rgb vs FP32 within 3e-2 (BF16) /
+4e-3 (FP16) abs; rendered rgb vs the FP64 oracle within 1e-2 (BF16) / 1e-3
+(FP16) max abs."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import native as orc
+from oracle import torch_ref
+
+pytestmark = pytest.mark.gpu
+TOL_SEG = {"bf16": 3e-2, "fp16": 4e-3}
+TOL_RGB = {"bf16": 1e-2, "fp16": 1e-3}
+
+
+def small():
+    from diver_gb300 import scenes
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.small_scene("cpu")
+    o, v = scenes.small_view("cpu")
+    return sc, o, v, DIVeRField.from_scene(sc, "cuda")
+
+
+def test_kmajor_layout_is_a_permutation():
+    from diver_gb300.decoder import _kmajor_index
+
+    for N, K in ((16, 32), (48, 32), (80, 64), (64, 64)):
+        idx = _kmajor_index(N, K)
+        assert torch.equal(idx.sort().values, torch.arange(N * K))
+
+
+@pytest.mark.parametrize("kind,channels", [("diver32", 32), ("diver64", 32), ("diver64", 64)])
+@pytest.mark.parametrize("form", ["bf16", "fp16"])
+def test_tc_segments_match_fp32(kind, channels, form):
+    from diver_gb300 import masked_segments, scenes
+    from diver_gb300.decoder import pack_plain, random_decoder
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.small_scene("cpu")
+    feats = scenes.features(65, channels, 0.05, 0, "cpu")
+    dec = random_decoder(kind, channels, 2)
+    dec.layers[dec.n_mlp1 - 1][1][0] += 0.6  # active density
+    field = DIVeRField(feats.cuda(), dec, sc.mask.cuda(), sc.xyzmin, sc.voxel_size)
+    o, v = scenes.small_view("cuda")
+    seg = field.segments(o, v)
+    from diver_gb300 import _native as N
+    from diver_gb300.renderer import KIND_ID
+
+    k = KIND_ID[kind]
+    W = 32 if kind == "diver32" else 64
+    pe_feat = torch.empty(o.shape[0], 28, device="cuda")
+    pe_out = torch.empty(o.shape[0], W, device="cuda")
+    st = N.stream()
+    N.call("dv_ray_pe", k, channels, N.ptr(field.params), o.shape[0], N.ptr(v), N.ptr(pe_feat), N.ptr(pe_out), st)
+    ref = torch.empty(seg.total, 4, device="cuda")
+    N.call("dv_decode_fwd", k, channels, N.ptr(field.params), N.ptr(field.voxels), 65, 65, 65, N.ptr(seg.seg),
+           N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(ref), st)
+    tcw = field.tc_weights(form)
+    got = torch.empty_like(ref)
+    tcw.decode(k, channels, field.voxels, seg, pe_out, got, st)
+    torch.cuda.synchronize()
+    assert int(tcw.err.item()) == 0
+    err = (got - ref).abs().max(0).values.cpu().numpy()
+    scale = ref.abs().max(0).values.cpu().numpy()
+    assert err[0] <= TOL_SEG[form] * max(1.0, scale[0]), (err, scale)
+    assert err[1:].max() <= TOL_SEG[form], (err, scale)
+
+
+@pytest.mark.parametrize("form", ["bf16", "fp16"])
+def test_tc_render_error_vs_fp64_oracle(form):
+    sc, o, v, field = small()
+    with torch.no_grad():
+        rgb, _ = field(o.cuda(), v.cuda(), form=form)
+    inter, num, _ = orc.masked_walk(o.numpy(), v.numpy(), sc.xyzmin, 64, sc.voxel_size, sc.mask.numpy(), 1.0)
+    segs = torch.from_numpy(orc.csr_from_padded(inter, num)).double()
+    ray = torch.from_numpy(np.repeat(np.arange(len(num)), num))
+    L = [(w.double(), b.double()) for w, b in sc.decoder.layers]
+    ref, _, _ = torch_ref.forward(sc.features.double(), L, 3, segs, ray, torch.from_numpy(num), v.double())
+    err = np.abs(rgb.cpu().numpy() - ref.numpy()).max()
+    assert err <= TOL_RGB[form], err
