@@ -257,26 +257,30 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     e2e_ms = allreduce_max(t0.elapsed_time(t1), world)
     e2e_val = rays / (e2e_ms * 1e-3) / 1e6
-    # ---- render: full frames, forward only ----
+    # ---- render: full frames, forward only, per decoder form ----
     render = None
     if not args.no_render:
-        times = []
+        render = {"resolution": [800, 800], "forms": {}}
         with torch.no_grad():
-            for k in range(2 + args.frames):
-                o, d = frame_rays(scene, k, dev)
-                torch.cuda.synchronize()
-                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                s.record()
-                field(o, d)
-                e.record()
-                torch.cuda.synchronize()
-                if k >= 2:
-                    times.append(s.elapsed_time(e))
-        times.sort()
-        p50 = statistics.median(times)
-        p99 = times[min(len(times) - 1, int(round(0.99 * (len(times) - 1))))]
-        render = {"form": "plain_fp32", "resolution": [800, 800], "Mrays_per_s": 640000 / (p50 * 1e-3) / 1e6,
-                  "p50_ms": p50, "p99_ms": p99, "frames": len(times)}
+            for form in ("fp32", "bf16", "fp16"):
+                times = []
+                for k in range(2 + args.frames):
+                    o, d = frame_rays(scene, k, dev)
+                    torch.cuda.synchronize()
+                    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    s.record()
+                    field(o, d, form=form)
+                    e.record()
+                    torch.cuda.synchronize()
+                    if k >= 2:
+                        times.append(s.elapsed_time(e))
+                times.sort()
+                p50 = statistics.median(times)
+                p99 = times[min(len(times) - 1, int(round(0.99 * (len(times) - 1))))]
+                render["forms"][form] = {"Mrays_per_s": 640000 / (p50 * 1e-3) / 1e6, "p50_ms": p50, "p99_ms": p99,
+                                         "frames": len(times)}
+        f = render["forms"]
+        render["bf16_speedup_vs_fp32"] = f["bf16"]["Mrays_per_s"] / f["fp32"]["Mrays_per_s"]
     # ---- roofline of the dominant kernel ----
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     tot = {k: sum(v) for k, v in kernel_ms.items()}
