@@ -225,6 +225,23 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
   if (warp == 0) tc::tmem_dealloc(tmem, NCOLS);
 }
 
+// CTAs of 128 threads that fit on one SM, from the kernel's registers and
+// shared memory, and never more than TMEM (512 columns) can hold.  (The
+// occupancy API under-reports kernels that allocate TMEM.)
+static int resident_ctas(const void* kernel, size_t dyn_smem, int ncols) {
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
+  int dev = 0, regs_sm = 65536, smem_sm = 228 * 1024, thr_sm = 2048;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  const int regs = std::max(fa.numRegs, 1) * 128;
+  const size_t smem = dyn_smem + fa.sharedSizeBytes + 1024;  // + per-CTA reservation
+  int n = std::min({thr_sm / 128, regs_sm / regs, (int)(smem_sm / smem), 512 / ncols});
+  return std::max(n, 1);
+}
+
 template <int C, int W, int D1, int BF16>
 int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   constexpr int NCOLS = W == 32 ? 64 : 128;
@@ -232,11 +249,10 @@ int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   const size_t smem = (size_t)a.wbytes + (size_t)a.nbias * 4 + 128 * KMAX * 2 + 16;
   auto k = decode_fwd_tc<C, W, D1, BF16, NCOLS>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
-  int per_sm = 0, dev = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, smem);
+  int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  per_sm = std::min(per_sm, 512 / NCOLS);  // never oversubscribe TMEM
+  const int per_sm = resident_ctas(reinterpret_cast<const void*>(k), smem, NCOLS);
   if (per_sm < 1) return DV_ERR_UNSUPPORTED;
   const long long tiles = (a.S + 127) / 128;
   const long long grid = std::min<long long>(tiles, (long long)sms * per_sm);
