@@ -33,6 +33,8 @@ SIGNATURES = {
     "dv_dense_pair_counts": (I32, [I32, P, P, P]),
     "dv_scan_scratch_bytes": (I64, [I64]),
     "dv_exclusive_scan": (I32, [P, I64, P, P, P]),
+    "dv_exclusive_scan_static_max": (I64, []),
+    "dv_exclusive_scan_static": (I32, [P, I64, P, P]),
     "dv_integrate_fwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_integrate_bwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_decoder_param_count": (I32, [I32, I32]),

@@ -10,6 +10,7 @@
 // segment-parallel decoder never touches padding; max(count) is reduced per
 // warp before one atomic; launches are stream-ordered with no device sync.
 #include "common.cuh"
+#include "scan.cuh"
 
 namespace dv {
 
@@ -285,9 +286,6 @@ __global__ void pair_counts_kernel(int batch, const int* __restrict__ num, int* 
 }
 
 // ---- exclusive scan: int32 counts -> int64 offsets --------------------------
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __device__ __forceinline__ long long block_exclusive_scan(long long x, long long* smem, long long* total) {
   // warp inclusive scan, then scan of warp totals

@@ -215,6 +215,23 @@ DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob,
                             const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
                             int* err, void* stream);
 
+/*
+ * Allocation-free form of dv_exclusive_scan (no counterpart in the reference,
+ * which allocates all its buffers with torch).  For callers that cannot
+ * allocate device memory themselves — an embedding host whose allocator owns
+ * the device, a frame loop with a fixed memory budget, code running while a
+ * CUDA graph is captured.  The tile sums live in a 32 KiB array inside the
+ * library (present on every device that loads it, until the process exits).
+ * n may be at most dv_exclusive_scan_static_max() (8,388,608 counts); larger
+ * n returns DV_ERR_OVERFLOW without launching anything.  The first call on a
+ * device looks up the array's address (once per device, with that device
+ * current): make it before any stream capture.  Calls share the array, so
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * Calls no cudaMalloc/cudaFree.
+ */
+DV_API long long dv_exclusive_scan_static_max(void);
+DV_API int dv_exclusive_scan_static(const int* counts, long long n, int64_t* offsets, void* stream);
+
 /* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.
  * ------------------------------------------------------------------------ */
