@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--frames", type=int, default=8)
     p.add_argument("--no-render", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--requests", type=int, default=24)
     return p.parse_args()
 
 
@@ -281,6 +283,10 @@ def run_ours(args, rank, world, local):
                                          "frames": len(times)}
         f = render["forms"]
         render["bf16_speedup_vs_fp32"] = f["bf16"]["Mrays_per_s"] / f["fp32"]["Mrays_per_s"]
+    # ---- serving: 4 resident scenes, Poisson arrivals at 200 req/s ----
+    serving = None
+    if not args.no_serving and world == 1:
+        serving = run_serving(args, dev)
     # ---- roofline of the dominant kernel ----
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     tot = {k: sum(v) for k, v in kernel_ms.items()}
@@ -307,12 +313,54 @@ def run_ours(args, rank, world, local):
         "gpu_launches": OUR_LAUNCHES_PER_STEP * args.steps,
         "roofline": roofline,
         "render": render,
+        "serving": serving,
         "segments_per_step": statistics.mean(seg_counts),
     }
     line["clocks"] = clk.summary()
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, batches[args.warmup], sample=256, repeats=3)
     return line
+
+
+def run_serving(args, dev):
+    """Two 256^3x32 DIVeR32 and two 256^3x64 DIVeR64 scenes (different seeds) under a
+    60 GB HBM budget; requests: scene id, a random camera on a radius-4 sphere and a
+    resolution from {200^2, 400^2, 800^2, 1280x720, 1920x1080}, Poisson arrivals at
+    200 req/s; BF16 tensor-core decoder."""
+    import torch
+
+    from diver_gb300 import scenes
+    from diver_gb300.renderer import DIVeRField
+    from diver_gb300.serving import GpuRenderer, Request, Residency, latency_summary, serve
+
+    specs = [("d32a", 32, "diver32", 0), ("d32b", 32, "diver32", 1), ("d64a", 64, "diver64", 2),
+             ("d64b", 64, "diver64", 3)]
+    res = Residency(60 << 30)
+    for name, ch, kind, k in specs:
+        nbytes = 257 ** 3 * ch * 4 + 256 ** 3
+        res.register(name, nbytes, lambda ch=ch, kind=kind, k=k: DIVeRField.from_scene(
+            scenes.grid_scene(256, ch, kind, device=dev, seed_offset=100 * k), dev))
+    for name, *_ in specs:  # load everything before the clock starts
+        res.acquire(name)
+        res.release(name)
+    g = torch.Generator().manual_seed(4)
+    sizes = [(200, 200), (400, 400), (800, 800), (720, 1280), (1080, 1920)]
+    t = 0.0
+    reqs = []
+    for i in range(args.requests):
+        t += float(torch.empty(1).exponential_(200.0, generator=g))
+        name = specs[int(torch.randint(0, 4, (1,), generator=g))][0]
+        H, W = sizes[int(torch.randint(0, 5, (1,), generator=g))]
+        v = torch.randn(3, generator=g)
+        c2w = scenes.look_at(v / v.norm() * 4.0)
+        reqs.append(Request(i, name, c2w, H, W, 1.2 * W, arrival=t))
+    torch.cuda.synchronize()
+    done = serve(reqs, res, GpuRenderer("bf16"), realtime=True, max_rays_in_flight=1 << 23, chunk_rays=1 << 19)
+    torch.cuda.synchronize()
+    out = latency_summary(done)
+    out.update({"scenes": len(specs), "arrival_rate_per_s": 200, "hbm_budget_gb": 60, "form": "bf16",
+                "resident_gb": res.used / 1e9})
+    return out
 
 
 # --- CPU reference path (oracle port) ------------------------------------------
