@@ -38,6 +38,9 @@ L_S = 1e-5
 #   decoder backward 4224 (input grads) + 5088 (weight grads incl. PE rows)
 #                    + 256 (integral) + 256 (corner scatter) + 4224 (recompute)
 FLOP_PER_SEG = {"dv_decode_fwd": 2 * (4224 + 256), "dv_decode_bwd": 2 * (4224 + 5088 + 256 + 256 + 4224 + 256)}
+# DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum + dram__bytes_write.sum,
+# one ncu capture of a training step of this workload, ~1.0 M segments; profiles/)
+TRAFFIC_PER_LAUNCH = {"dv_decode_bwd": 1157349888 + 505501184}
 OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd, composite_fwd, composite_bwd, decode_bwd
 
 
@@ -296,7 +299,7 @@ def run_ours(args, rank, world, local):
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     achieved = flops / (avg_ms * 1e-3) / 1e12 if flops else None
     roofline = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC_PER_LAUNCH.get(dom),
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (measured)" if peaks else "fallback",
                 "avg_launch_ms": avg_ms, "segments_per_launch": statistics.mean(seg_counts),
                 "kernel_share": {k: v / sum(tot.values()) for k, v in tot.items()}}
