@@ -41,7 +41,10 @@ FLOP_PER_SEG = {"dv_decode_fwd": 2 * (4224 + 256), "dv_decode_bwd": 2 * (4224 + 
 # DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum + dram__bytes_write.sum,
 # one ncu capture of a training step of this workload, ~1.0 M segments; profiles/)
 TRAFFIC_PER_LAUNCH = {"dv_decode_bwd": 1157349888 + 505501184}
-OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd, composite_fwd, composite_bwd, decode_bwd
+FLOP_PER_SEG["dv_decode_bwd_tc"] = FLOP_PER_SEG["dv_decode_bwd"]
+FLOP_PER_SEG["dv_decode_fwd_tc"] = FLOP_PER_SEG["dv_decode_fwd"]
+OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd(_tc), composite_fwd, composite_bwd,
+#                             decode_bwd(_tc)
 
 
 def parse():
@@ -55,6 +58,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--requests", type=int, default=24)
+    p.add_argument("--form", default="bf16", choices=["fp32", "bf16", "fp16"],
+                   help="decoder form of the headline training step (the FP32 form is always timed too)")
     return p.parse_args()
 
 
@@ -193,10 +198,10 @@ def make_batches(scene, count, device, seed=4):
     return out
 
 
-def train_step(field, o, d, tgt):
+def train_step(field, o, d, tgt, form="fp32"):
     import torch
 
-    rgb, reg = field(o, d)
+    rgb, reg = field(o, d, form=form)
     loss = torch.nn.functional.mse_loss(rgb, tgt) + L_S * reg
     gv, gp = torch.autograd.grad(loss, [field.voxels, field.params])
     return loss, gv, gp
@@ -221,32 +226,35 @@ def run_ours(args, rank, world, local):
     scene = train_scene(dev)
     field = DIVeRField.from_scene(scene, dev)
     batches = make_batches(scene, args.warmup + args.steps, dev)
-    # warm-up
-    for i in range(args.warmup):
-        train_step(field, *batches[i])
-    torch.cuda.synchronize()
-    # ---- timed: device-resident inputs ----
-    R.KERNEL_EVENTS = {}
-    barrier(world)
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record()
-        segs_total = 0
-        for i in range(args.steps):
-            o, d, tgt = batches[args.warmup + i]
-            train_step(field, o, d, tgt)
-        end.record()
+    forms = {}
+    for form in ("fp32", args.form) if args.form != "fp32" else ("fp32",):
+        for i in range(args.warmup):
+            train_step(field, *batches[i], form=form)
         torch.cuda.synchronize()
-    barrier(world)
-    ms = start.elapsed_time(end)
-    kernel_ms = {k: [s.elapsed_time(e) for s, e in v] for k, v in R.KERNEL_EVENTS.items()}
-    R.KERNEL_EVENTS = None
+        R.KERNEL_EVENTS = {}
+        barrier(world)
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record()
+            for i in range(args.steps):
+                o, d, tgt = batches[args.warmup + i]
+                train_step(field, o, d, tgt, form=form)
+            end.record()
+            torch.cuda.synchronize()
+        barrier(world)
+        kms = {k: [s.elapsed_time(e) for s, e in v] for k, v in R.KERNEL_EVENTS.items()}
+        R.KERNEL_EVENTS = None
+        forms[form] = (start.elapsed_time(end), kms, clk.summary())
+    form = args.form
+    ms, kernel_ms, clocks = forms[form]
     # segments per step (for the roofline): recount with the same traversal
     seg_counts = [field.segments(*batches[args.warmup + i][:2]).total for i in range(args.steps)]
     ms_max = allreduce_max(ms, world)
     rays = allreduce_sum(float(BATCH * args.steps), world)
     value = rays / (ms_max * 1e-3) / 1e6
+    train_forms = {f: {"Mrays_per_s": rays / (allreduce_max(v[0], world) * 1e-3) / 1e6,
+                       "ms_per_step": v[0] / args.steps} for f, v in forms.items()}
     # ---- e2e: pinned host inputs, H2D + D2H inside the timed region ----
     host = [tuple(t.cpu().pin_memory() for t in b) for b in batches[args.warmup:]]
     torch.cuda.synchronize()
@@ -256,7 +264,7 @@ def run_ours(args, rank, world, local):
     t0.record()
     for o_h, d_h, g_h in host:
         o, d, tgt = (x.to(dev, non_blocking=True) for x in (o_h, d_h, g_h))
-        loss, _, _ = train_step(field, o, d, tgt)
+        loss, _, _ = train_step(field, o, d, tgt, form=form)
         loss.item()
     t1.record()
     torch.cuda.synchronize()
@@ -306,20 +314,24 @@ def run_ours(args, rank, world, local):
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32",
+        "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp16": "f16"}[form],
         "data": "synthetic: seeded 256^3x32 grid N(0,0.02^2), 16-blob occupancy ~60%, 100 cameras 800x800, "
                 "targets U[0,1]",
         "config": {"workload": "train fwd+bwd, DIVeR32, 256^3 x 32 features, batch 4096 rays that hit occupied voxels",
-                   "global_batch": BATCH * world, "form": "plain_fp32", "parallelism": f"replicas x{world}",
+                   "global_batch": BATCH * world,
+                   "form": "plain FP32" if form == "fp32" else f"tcgen05 {form.upper()} decoder fwd+bwd, FP32 accumulation, "
+                           "FP32 integration/compositing/weight-gradient accumulation",
+                   "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (2.2 GB grid), a fresh batch every step"},
         "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": BATCH * 9 * 4, "d2h_bytes_per_step": 4},
         "gpu_launches": OUR_LAUNCHES_PER_STEP * args.steps,
         "roofline": roofline,
+        "train_forms": train_forms,
         "render": render,
         "serving": serving,
         "segments_per_step": statistics.mean(seg_counts),
     }
-    line["clocks"] = clk.summary()
+    line["clocks"] = clocks
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, batches[args.warmup], sample=256, repeats=3)
     return line

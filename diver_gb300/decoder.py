@@ -240,3 +240,33 @@ def pack_tc(dec: Decoder, bf16: bool = True):
         off += N * K * 2
         boff += N
     return torch.cat(images), torch.cat(biases).float(), torch.tensor(table, dtype=torch.int32)
+
+
+def tc_bwd_matrices(dec: Decoder):
+    """Transposed weights for the tensor-core backward (DIVeR32): per layer
+    W^T as [N = in][K = out padded to 16], the mlp1 output layer in the torch
+    order (sigma first), so delta @ W^T gives the input gradient."""
+    if dec.kind != "diver32":
+        raise ValueError("the tensor-core backward is implemented for DIVeR32")
+    W = dec.width
+    (w0, _), (w1, _), (w2, _), (w3, _), (w4, _) = [(w.detach().float().cpu(), b) for w, b in dec.layers]
+    m2 = torch.zeros(W, W + 16)
+    m2[:, :W + 1] = w2.t()
+    m4 = torch.zeros(W, 16)
+    m4[:, :3] = w4.t()
+    return [w0.t().contiguous(), w1.t().contiguous(), m2, w3[:, :W].t().contiguous(), m4]
+
+
+def pack_tc_bwd(dec: Decoder, bf16: bool = True):
+    """(blob uint8, layers int32 [n, 3] = (byte offset, K, N)) of tc_bwd_matrices."""
+    dt = torch.bfloat16 if bf16 else torch.float16
+    images, table = [], []
+    off = 0
+    for m in tc_bwd_matrices(dec):
+        N, K = m.shape
+        img = torch.zeros(N * K, dtype=dt)
+        img[_kmajor_index(N, K)] = m.reshape(-1).to(dt)
+        images.append(img.view(torch.uint8))
+        table.append([off, K, N])
+        off += N * K * 2
+    return torch.cat(images), torch.tensor(table, dtype=torch.int32)

@@ -20,7 +20,7 @@ import torch
 from torch.autograd import Function
 
 from . import _native as N
-from .decoder import Decoder, pack_plain, pack_tc
+from .decoder import Decoder, pack_plain, pack_tc, pack_tc_bwd
 from .ray_voxel_intersection import Segments, dense_segments, masked_segments
 
 KIND_ID = {"diver32": 32, "diver64": 64}
@@ -70,6 +70,23 @@ class TcWeights:
         self.table = table.contiguous()
         self.bf16 = bool(bf16)
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
+        self.bwd = None
+        if decoder.kind == "diver32" and decoder.channels == 32:
+            wb, tb = pack_tc_bwd(decoder, bf16)
+            self.bwd = (wb.to(device), tb.contiguous())
+
+    def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st) -> bool:
+        """Tensor-core backward; False when this decoder has none (the caller
+        then runs the FP32 backward)."""
+        if self.bwd is None:
+            return False
+        nx, ny, nz, c = _grid(voxels)
+        wb, tb = self.bwd
+        _timed("dv_decode_bwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
+               self.bias.numel(), self.table.data_ptr(), N.ptr(wb), wb.numel(), tb.data_ptr(), tb.shape[0],
+               N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, N.ptr(pe_feat), N.ptr(pe_out),
+               N.ptr(d4), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
+        return True
 
     def decode(self, kind, channels, voxels, seg, pe_out, out4, st):
         nx, ny, nz, c = _grid(voxels)
@@ -105,7 +122,7 @@ class SegmentRender(Function):
         M = max(seg.max_count, 1)
         reg_mean = reg.sum() / float(B * M)
         ctx.save_for_backward(voxels, params, dirs, pe_feat, pe_out, out4, rgb)
-        ctx.seg, ctx.kind, ctx.BM = seg, kind, float(B * M)
+        ctx.seg, ctx.kind, ctx.BM, ctx.tc = seg, kind, float(B * M), tc
         return rgb, reg_mean
 
     @staticmethod
@@ -122,6 +139,8 @@ class SegmentRender(Function):
         _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb), reg_coef, N.ptr(d4), st)
         gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
+        if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st):
+            return gv, gp, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
         return gv, gp, None, None, None, None, None

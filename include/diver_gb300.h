@@ -232,6 +232,22 @@ DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob,
 DV_API long long dv_exclusive_scan_static_max(void);
 DV_API int dv_exclusive_scan_static(const int* counts, long long n, int64_t* offsets, void* stream);
 
+/*
+ * Tensor-core form of dv_decode_bwd (DIVeR32, 32 channels): recomputes the
+ * forward on tcgen05 with the images of dv_decode_fwd_tc (wf, f_layers rows
+ * of 4 ints), propagates deltas through wb, the transposed weights
+ * [N = in][K = out padded to 16] per layer (b_layers: HOST rows of
+ * (byte offset, K, N)); weight gradients accumulate in FP32 from BF16/FP16
+ * activations and deltas.  Returns DV_ERR_UNSUPPORTED for other decoders.
+ */
+DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_bytes,
+                            const float* bias, int nbias, const int* f_layers, const void* wb,
+                            int wb_bytes, const int* b_layers, int n_layers, const float* voxels,
+                            int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
+                            long long n_seg, const float* pe_feat, const float* pe_out,
+                            const float* d4, float* grad_voxels, float* grad_params, int* err,
+                            void* stream);
+
 /* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.
  * ------------------------------------------------------------------------ */

@@ -82,3 +82,56 @@ def test_tc_render_error_vs_fp64_oracle(form):
     ref, _, _ = torch_ref.forward(sc.features.double(), L, 3, segs, ray, torch.from_numpy(num), v.double())
     err = np.abs(rgb.cpu().numpy() - ref.numpy()).max()
     assert err <= TOL_RGB[form], err
+
+
+# Stated tolerances for the tensor-core training form (BF16 / FP16 operands,
+# FP32 accumulation): gradients within these relative L2 errors of the FP32
+# backward, per tensor.
+TOL_GRAD = {"bf16": 3e-2, "fp16": 5e-3}
+
+
+@pytest.mark.parametrize("form", ["bf16", "fp16"])
+def test_tc_backward_matches_fp32_backward(form, golden):
+    from diver_gb300 import masked_segments
+    from diver_gb300.decoder import pack_plain
+    from diver_gb300.renderer import TcWeights, render_segments
+    from tests.test_decode_gpu import decoder_from_golden
+
+    g = golden("decode_ref.npz")
+    dec = decoder_from_golden(g, "diver32")
+    o = torch.from_numpy(g["o_hit"]).cuda()
+    d = torch.from_numpy(g["d_hit"]).cuda()
+    seg = masked_segments(o, d, -1.5, 12, 0.25, torch.from_numpy(g["mask"]).cuda(), 1.0)
+    tgt = torch.from_numpy(g["target"]).cuda()
+    grads = {}
+    for f in ("fp32", form):
+        vox = torch.from_numpy(g["voxels"]).cuda().requires_grad_(True)
+        params = pack_plain(dec).cuda().requires_grad_(True)
+        tc = None if f == "fp32" else TcWeights(dec, "cuda", bf16=(f == "bf16"))
+        rgb, reg = render_segments(vox, params, seg, d, "diver32", True, tc)
+        (torch.nn.functional.mse_loss(rgb, tgt) + 1e-5 * reg).backward()
+        torch.cuda.synchronize()
+        if tc is not None:
+            assert int(tc.err.item()) == 0
+        grads[f] = (vox.grad.clone(), params.grad.clone())
+    for a, b in zip(grads[form], grads["fp32"]):
+        rel = ((a - b).norm() / b.norm()).item()
+        assert rel <= TOL_GRAD[form], rel
+
+
+def test_tc_backward_on_the_small_scene_runs_full_tiles():
+    """Many tiles (64^3 scene, 200x200 view): tensor-core grads vs FP32 grads."""
+    from diver_gb300 import scenes
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.small_scene("cpu")
+    o, v = scenes.small_view("cuda")
+    tgt = torch.rand(o.shape[0], 3, generator=torch.Generator().manual_seed(1)).cuda()
+    out = {}
+    for form in ("fp32", "fp16"):
+        field = DIVeRField.from_scene(sc, "cuda")
+        rgb, reg = field(o, v, form=form)
+        (torch.nn.functional.mse_loss(rgb, tgt) + 1e-5 * reg).backward()
+        out[form] = (field.voxels.grad.clone(), field.params.grad.clone())
+    for a, b in zip(out["fp16"], out["fp32"]):
+        assert ((a - b).norm() / b.norm()).item() <= TOL_GRAD["fp16"]
