@@ -246,8 +246,8 @@ def run_ours(args, rank, world, local):
         kms = {k: [s.elapsed_time(e) for s, e in v] for k, v in R.KERNEL_EVENTS.items()}
         R.KERNEL_EVENTS = None
         forms[form] = (start.elapsed_time(end), kms, clk.summary())
-    form = args.form
-    ms, kernel_ms, clocks = forms[form]
+    tform = args.form
+    ms, kernel_ms, clocks = forms[tform]
     # segments per step (for the roofline): recount with the same traversal
     seg_counts = [field.segments(*batches[args.warmup + i][:2]).total for i in range(args.steps)]
     ms_max = allreduce_max(ms, world)
@@ -264,7 +264,7 @@ def run_ours(args, rank, world, local):
     t0.record()
     for o_h, d_h, g_h in host:
         o, d, tgt = (x.to(dev, non_blocking=True) for x in (o_h, d_h, g_h))
-        loss, _, _ = train_step(field, o, d, tgt, form=form)
+        loss, _, _ = train_step(field, o, d, tgt, form=tform)
         loss.item()
     t1.record()
     torch.cuda.synchronize()
@@ -314,12 +314,12 @@ def run_ours(args, rank, world, local):
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp16": "f16"}[form],
+        "vs_baseline": None, "dtype": {"fp32": "f32", "bf16": "bf16", "fp16": "f16"}[tform],
         "data": "synthetic: seeded 256^3x32 grid N(0,0.02^2), 16-blob occupancy ~60%, 100 cameras 800x800, "
                 "targets U[0,1]",
         "config": {"workload": "train fwd+bwd, DIVeR32, 256^3 x 32 features, batch 4096 rays that hit occupied voxels",
                    "global_batch": BATCH * world,
-                   "form": "plain FP32" if form == "fp32" else f"tcgen05 {form.upper()} decoder fwd+bwd, FP32 accumulation, "
+                   "form": "plain FP32" if tform == "fp32" else f"tcgen05 {tform.upper()} decoder fwd+bwd, FP32 accumulation, "
                            "FP32 integration/compositing/weight-gradient accumulation",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (2.2 GB grid), a fresh batch every step"},

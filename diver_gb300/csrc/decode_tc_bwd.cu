@@ -1,29 +1,27 @@
 // Tensor-core (tcgen05) backward of the decoder for DIVeR32 (32 channels,
-// width 32): per tile of 128 segments, recompute the forward on tcgen05
-// keeping every layer's activations, then propagate the deltas back through
-// the layers on tcgen05 (B operands = transposed weight images), accumulate
-// the weight gradients on the CUDA cores, and scatter the feature gradient
-// into the 8 corner rows of every segment.
+// width 32), BF16 operands: per tile of 128 segments, recompute the forward
+// on tcgen05 keeping every layer's activations, then per layer (last first)
+//   - propagate the delta:  dL/d input = delta @ W      (MMA, B = W^T image)
+//   - weight gradient:      dW += delta^T @ activation  (MMA over the tile's
+//     128 segments, both operands read transposed (MN-major) from the same
+//     tiles; FP32 accumulators stay in TMEM for the CTA's whole life)
+//   - bias gradient:        sum of the delta column (CUDA cores, registers)
+// and finally scatter the feature gradient into the 8 corner rows of every
+// segment with vector atomics.  Weight and bias gradients are added to the
+// packed torch-layout gradient once per CTA.
 //
-// Shared memory (bytes; 2 CTAs per SM):
-//   Bf  forward weight images   [N][K] K-major, per layer     10240
-//   Bb  backward weight images  [N=in][K=out] K-major (W^T)   10240
-//   bias                        forward biases (tensor-core order)
-//   K   operand tile 128 x 48   K-major (forward A, backward delta)
-//   R0, R1, R2, RH, R4          row-major activations: feature, relu(h0),
-//                               relu(h1), (hidden | PE), relu(mlp2 hidden)
-//   D   row-major delta tile 128 x 48
-// The weight gradient of the CTA lives in registers: each thread owns
-// 2-row x 4-column chunks of the packed torch layout (W^T [in][out4], bias),
-// accumulates sum_s act[s][i] * delta[s][j] over every tile, and adds them to
-// grad_params with atomics once at the end.
+// Shared memory (bytes; 2 CTAs per SM): forward weight images (10240),
+// transposed weight images (10240), forward biases, activation tiles X0, A1,
+// A2 (128 x 32), HP (128 x 64: hidden | PE | zeros), A4 (128 x 32), and the
+// delta tile (128 x 128, columns past the layer's width are zero or ignored),
+// all in the 8x8 core-matrix layout; FP32 staging of the feature gradient
+// aliases A1..HP.  TMEM: 64 working columns + 192 columns of weight
+// gradients (256).
 // Reference semantics: the autograd backward of model/diver.py:159-180.
 #include "common.cuh"
 #include "integrate.cuh"
 #include "mlp.cuh"
 #include "tc.cuh"
-
-#include <cuda_fp16.h>
 
 #include <algorithm>
 
@@ -32,20 +30,16 @@ namespace dv {
 namespace bw {
 
 constexpr int C = 32, W = 32;
-constexpr int KK = W + 16;      // widest operand K (mlp1 output delta: 33 -> 48)
-constexpr int SH = W + 32;      // row stride of RH: hidden (W) | PE (27) | zeros
-constexpr int SD = KK;          // row stride of the delta tile
+constexpr int FH = 64;          // columns of HP: hidden (W) | PE (27) | zeros
+constexpr int FD = 128;         // columns of the delta tile (the weight-gradient MMA's M)
 constexpr int NL = 5;
+constexpr int TMEM_COLS = 256;
 // layer: 0 (C->W), 1 (W->W), 2 (W->W+1: sigma, hidden), 3 (W+27->W), 4 (W->3)
 __host__ __device__ constexpr int IN(int l) { return l == 0 ? C : (l == 3 ? W + PE_DIM : W); }
-__host__ __device__ constexpr int INP(int l) { return l == 0 ? C : (l == 3 ? W + PE_PAD : W); }  // even
 __host__ __device__ constexpr int OUT(int l) { return l == 2 ? W + 1 : (l == 4 ? 3 : W); }
 __host__ __device__ constexpr int OUT4(int l) { return pad4(OUT(l)); }
-__host__ __device__ constexpr int Q(int l) { return OUT4(l) / 4; }
-__host__ __device__ constexpr int P(int l) { return INP(l) / 2 + 1; }  // pair rows incl. the bias pair
-__host__ __device__ constexpr int BEGIN(int l) { return l == 0 ? 0 : BEGIN(l - 1) + P(l - 1) * Q(l - 1); }
-constexpr int CHN = BEGIN(NL);
-constexpr int SLOTS = (CHN + 127) / 128;
+__host__ __device__ constexpr int NIN(int l) { return l == 3 ? FH : C; }  // weight-gradient MMA N (in, padded)
+__host__ __device__ constexpr int DWCOL(int l) { return l == 0 ? 64 : (l <= 3 ? DWCOL(l - 1) + NIN(l - 1) : 224); }
 
 struct Args {
   const float* grid;
@@ -71,74 +65,62 @@ struct Args {
 };
 
 struct Smem {
-  uint8_t* Bf;
-  uint8_t* Bb;
+  uint8_t *Bf, *Bb;
   float* bias;
-  uint8_t* K;
-  uint16_t *R0, *R1, *R2, *RH, *R4, *D;
-  float* stage;  // fp32 [128][C+4], aliases R1..RH
+  uint8_t *X0, *A1, *A2, *HP, *A4, *D;
+  float* stage;  // fp32 [128][C+4], aliases A1..HP
   uint64_t* bar;
   uint32_t* tslot;
 };
 
-template <int BF16>
-__device__ __forceinline__ float lo16(uint32_t w) {
-  if (BF16) return __uint_as_float(w << 16);
-  return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu)));
-}
-template <int BF16>
-__device__ __forceinline__ float hi16(uint32_t w) {
-  if (BF16) return __uint_as_float(w & 0xffff0000u);
-  return __half2float(__ushort_as_half((unsigned short)(w >> 16)));
-}
-
-// Writes n (multiple of 8) values of row t at columns c0.. : into the K-major
-// operand (K = kdim) when Kt != null, and into the row-major copy rowp (the
-// row's start) when rowp != null.
-template <int BF16>
-__device__ __forceinline__ void put_row(uint8_t* Kt, int kdim, uint16_t* rowp, int t, const float* v, int n,
-                                        int c0 = 0) {
+// Writes n (multiple of 8) values of row t at columns c0.. of a tile with F columns.
+__device__ __forceinline__ void put_row(uint8_t* tile, int F, int t, const float* v, int n, int c0 = 0) {
 #pragma unroll
   for (int c = 0; c < n; c += 8) {
     uint4 w;
-    w.x = tc::pack2<BF16>(v[c], v[c + 1]);
-    w.y = tc::pack2<BF16>(v[c + 2], v[c + 3]);
-    w.z = tc::pack2<BF16>(v[c + 4], v[c + 5]);
-    w.w = tc::pack2<BF16>(v[c + 6], v[c + 7]);
-    if (Kt) *reinterpret_cast<uint4*>(Kt + tc::kmajor_offset(t, c0 + c, kdim)) = w;
-    if (rowp) *reinterpret_cast<uint4*>(rowp + c0 + c) = w;
+    w.x = tc::pack2<1>(v[c], v[c + 1]);
+    w.y = tc::pack2<1>(v[c + 2], v[c + 3]);
+    w.z = tc::pack2<1>(v[c + 4], v[c + 5]);
+    w.w = tc::pack2<1>(v[c + 6], v[c + 7]);
+    *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(t, c0 + c, F)) = w;
   }
 }
 
-template <int BF16>
-__device__ __forceinline__ void get_row(const uint16_t* rowp, float* v, int n) {
+// ReLU mask of row t (first n columns) of a BF16 tile: m[i] = act > 0.
+__device__ __forceinline__ void relu_mask(const uint8_t* tile, int F, int t, float* v, int n) {
 #pragma unroll
   for (int c = 0; c < n; c += 8) {
-    const uint4 w = *reinterpret_cast<const uint4*>(rowp + c);
-    v[c] = lo16<BF16>(w.x);
-    v[c + 1] = hi16<BF16>(w.x);
-    v[c + 2] = lo16<BF16>(w.y);
-    v[c + 3] = hi16<BF16>(w.y);
-    v[c + 4] = lo16<BF16>(w.z);
-    v[c + 5] = hi16<BF16>(w.z);
-    v[c + 6] = lo16<BF16>(w.w);
-    v[c + 7] = hi16<BF16>(w.w);
+    const uint4 w = *reinterpret_cast<const uint4*>(tile + tc::kmajor_offset(t, c, F));
+    const uint32_t x[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!(__uint_as_float(x[j] << 16) > 0.f)) v[c + 2 * j] = 0.f;
+      if (!(__uint_as_float(x[j] & 0xffff0000u) > 0.f)) v[c + 2 * j + 1] = 0.f;
+    }
   }
 }
 
-template <int BF16>
-__device__ __forceinline__ void issue(const uint8_t* Bimg, int K, int N, const uint8_t* At, uint32_t tmem,
-                                      uint64_t* bar) {
-  if (threadIdx.x == 0) {
-    tc::fence_after_sync();
-    const uint32_t idesc = tc::idesc_f16(128, N, BF16);
-    const uint32_t a0 = tc::smem_u32(At), b0 = tc::smem_u32(Bimg);
-    const uint32_t sbo = (uint32_t)(K / 8) * 128;
-    for (int k = 0; k < K / 16; ++k)
-      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
-                  k > 0 ? 1u : 0u);
-    tc::mma_commit(bar);
-  }
+// Forward / propagation MMA: D[128][N] = A[128 rows][K] (K-major tile with F
+// columns) x B^T (B image [N][K]).
+__device__ __forceinline__ void mma_rows(uint32_t d_tmem, const uint8_t* A, int F, const uint8_t* B, int K, int N) {
+  const uint32_t idesc = tc::idesc_f16(128, N, 1);
+  const uint32_t a0 = tc::smem_u32(A), b0 = tc::smem_u32(B);
+  for (int k = 0; k < K / 16; ++k)
+    tc::mma_f16(d_tmem, tc::smem_desc(a0 + k * 256, 128, (uint32_t)(F / 8) * 128),
+                tc::smem_desc(b0 + k * 256, 128, (uint32_t)(K / 8) * 128), idesc, k > 0 ? 1u : 0u);
+}
+
+// Weight-gradient MMA over the tile's 128 segments: dW[128 = out][N = in] +=
+// delta^T x act, both operands MN-major views of the row tiles (LBO = stride of
+// 8 segments, SBO = stride of 8 features).
+__device__ __forceinline__ void mma_dw(uint32_t d_tmem, const uint8_t* Dt, const uint8_t* act, int Fact, int N,
+                                       bool accumulate) {
+  const uint32_t idesc = tc::idesc_f16(128, N, 1) | (1u << 15) | (1u << 16);
+  const uint32_t a0 = tc::smem_u32(Dt), b0 = tc::smem_u32(act);
+  const uint32_t lboA = (FD / 8) * 128, lboB = (uint32_t)(Fact / 8) * 128;
+  for (int k = 0; k < 8; ++k)
+    tc::mma_f16(d_tmem, tc::smem_desc(a0 + k * 2 * lboA, lboA, 128), tc::smem_desc(b0 + k * 2 * lboB, lboB, 128),
+                idesc, (accumulate || k > 0) ? 1u : 0u);
 }
 
 __device__ __forceinline__ bool wait_mma(uint64_t* bar, uint32_t& phase) {
@@ -154,52 +136,17 @@ __device__ __forceinline__ void sync_mma() {
   __syncthreads();
 }
 
-// dW chunks of layer L owned by this thread: sum over the tile's segments.
-template <int L, int BF16>
-__device__ __forceinline__ void accumulate(float (&acc)[SLOTS][8], const uint16_t* act, int act_stride,
-                                           const uint16_t* D) {
-#pragma unroll
-  for (int k = 0; k < SLOTS; ++k) {
-    const int c = threadIdx.x + 128 * k;
-    if (c < BEGIN(L) || c >= BEGIN(L + 1)) continue;
-    const int local = c - BEGIN(L);
-    const int p = local / Q(L), jq = local - p * Q(L);
-    const bool bias_row = (2 * p == INP(L));
-    float a[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) a[j] = acc[k][j];
-    if (bias_row) {
-#pragma unroll 4
-      for (int s = 0; s < 128; ++s) {
-        const uint2 d = *reinterpret_cast<const uint2*>(D + s * SD + 4 * jq);
-        a[0] += lo16<BF16>(d.x);
-        a[1] += hi16<BF16>(d.x);
-        a[2] += lo16<BF16>(d.y);
-        a[3] += hi16<BF16>(d.y);
-      }
-    } else {
-#pragma unroll 4
-      for (int s = 0; s < 128; ++s) {
-        const uint32_t x = *reinterpret_cast<const uint32_t*>(act + s * act_stride + 2 * p);
-        const uint2 d = *reinterpret_cast<const uint2*>(D + s * SD + 4 * jq);
-        const float x0 = lo16<BF16>(x), x1 = hi16<BF16>(x);
-        const float d0 = lo16<BF16>(d.x), d1 = hi16<BF16>(d.x), d2 = lo16<BF16>(d.y), d3 = hi16<BF16>(d.y);
-        a[0] = fmaf(x0, d0, a[0]);
-        a[1] = fmaf(x0, d1, a[1]);
-        a[2] = fmaf(x0, d2, a[2]);
-        a[3] = fmaf(x0, d3, a[3]);
-        a[4] = fmaf(x1, d0, a[4]);
-        a[5] = fmaf(x1, d1, a[5]);
-        a[6] = fmaf(x1, d2, a[6]);
-        a[7] = fmaf(x1, d3, a[7]);
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[k][j] = a[j];
+// Sum of column t of the delta tile over the 128 segments (bias gradient).
+__device__ __forceinline__ float column_sum(const uint8_t* Dt, int t) {
+  float s = 0.f;
+#pragma unroll 8
+  for (int r = 0; r < 128; ++r) {
+    const uint16_t h = *reinterpret_cast<const uint16_t*>(Dt + tc::kmajor_offset(r, t, FD));
+    s += __uint_as_float((uint32_t)h << 16);
   }
+  return s;
 }
 
-template <int BF16>
 __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   Smem m;
@@ -210,21 +157,19 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   p += a.wb_bytes;
   m.bias = reinterpret_cast<float*>(p);
   p += a.nbias * 4;
-  m.K = p;
-  p += 128 * KK * 2;
-  m.R0 = reinterpret_cast<uint16_t*>(p);
+  m.X0 = p;
   p += 128 * C * 2;
-  m.R1 = reinterpret_cast<uint16_t*>(p);
+  m.A1 = p;
   m.stage = reinterpret_cast<float*>(p);
   p += 128 * W * 2;
-  m.R2 = reinterpret_cast<uint16_t*>(p);
+  m.A2 = p;
   p += 128 * W * 2;
-  m.RH = reinterpret_cast<uint16_t*>(p);
-  p += 128 * SH * 2;
-  m.R4 = reinterpret_cast<uint16_t*>(p);
+  m.HP = p;
+  p += 128 * FH * 2;
+  m.A4 = p;
   p += 128 * W * 2;
-  m.D = reinterpret_cast<uint16_t*>(p);
-  p += 128 * SD * 2;
+  m.D = p;
+  p += 128 * FD * 2;
   m.bar = reinterpret_cast<uint64_t*>(p);
   m.tslot = reinterpret_cast<uint32_t*>(p + 8);
 
@@ -234,26 +179,25 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   for (int i = t; i < a.wb_bytes / 16; i += 128)
     reinterpret_cast<uint4*>(m.Bb)[i] = __ldg(reinterpret_cast<const uint4*>(a.wb) + i);
   for (int i = t; i < a.nbias; i += 128) m.bias[i] = __ldg(a.bias + i);
+  for (int i = t; i < 128 * FD * 2 / 16; i += 128) reinterpret_cast<uint4*>(m.D)[i] = make_uint4(0, 0, 0, 0);
+  for (int i = t; i < 128 * FH * 2 / 16; i += 128) reinterpret_cast<uint4*>(m.HP)[i] = make_uint4(0, 0, 0, 0);
   if (t == 0) {
     tc::mbar_init(m.bar, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
-    tc::tmem_alloc(m.tslot, 64);
+    tc::tmem_alloc(m.tslot, TMEM_COLS);
     tc::tmem_relinquish();
   }
   sync_mma();
   tc::fence_after_sync();
   const uint32_t tmem = *m.tslot;
-  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t lane = (uint32_t)(warp * 32) << 16;
+  const uint32_t trow = tmem + lane;
   uint32_t phase = 0;
-  bool ok = true;
-  float acc[SLOTS][8];
-#pragma unroll
-  for (int k = 0; k < SLOTS; ++k)
-#pragma unroll
-    for (int j = 0; j < 8; ++j) acc[k][j] = 0.f;
-  float v[KK];
+  bool ok = true, first = true;
+  float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float v[48];
 
   const long long tiles = (a.S + 127) / 128;
   for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
@@ -261,7 +205,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
     const long long s = s0 + t;
     const bool valid = s < a.S;
     const int ray = valid ? __ldg(a.seg_ray + s) : 0;
-    // ---- gather: feature rows (K-major operand + row-major copy) ----
+    // ---- gather: feature rows ----
     {
       constexpr int TPS = C / 4, SPP = 128 / TPS;
 #pragma unroll 1
@@ -275,59 +219,69 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
                                                __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
           f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
         }
-        const uint2 w = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
-        *reinterpret_cast<uint2*>(m.K + tc::kmajor_offset(ls, 4 * q, C)) = w;
-        *reinterpret_cast<uint2*>(m.R0 + ls * C + 4 * q) = w;
+        *reinterpret_cast<uint2*>(m.X0 + tc::kmajor_offset(ls, 4 * q, C)) =
+            make_uint2(tc::pack2<1>(f.x, f.y), tc::pack2<1>(f.z, f.w));
       }
     }
     sync_mma();
-    // ---- forward ----
-    // layer 0: relu(x0 W0^T + b0) -> R1
-    issue<BF16>(m.Bf + a.f_off[0], a.f_K[0], a.f_N[0], m.K, tmem, m.bar);
+    // ---- forward (activations kept) ----
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.X0, C, m.Bf + a.f_off[0], C, W);
+      tc::mma_commit(m.bar);
+    }
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     tc::ld_32x32b_x32(trow, v);
     tc::ld_wait();
 #pragma unroll
     for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[0] + i], 0.f);
-    put_row<BF16>(m.K, W, m.R1 + t * W, t, v, W);
+    put_row(m.A1, W, t, v, W);
     sync_mma();
-    // layer 1: relu(a1 W1^T + b1) -> R2
-    issue<BF16>(m.Bf + a.f_off[1], a.f_K[1], a.f_N[1], m.K, tmem, m.bar);
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.A1, W, m.Bf + a.f_off[1], W, W);
+      tc::mma_commit(m.bar);
+    }
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     tc::ld_32x32b_x32(trow, v);
     tc::ld_wait();
 #pragma unroll
     for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[1] + i], 0.f);
-    put_row<BF16>(m.K, W, m.R2 + t * W, t, v, W);
+    put_row(m.A2, W, t, v, W);
     sync_mma();
-    // layer 2 (mlp1 output): hidden (columns 0..W-1) -> RH[0..W); PE -> RH[W..)
-    issue<BF16>(m.Bf + a.f_off[2], a.f_K[2], a.f_N[2], m.K, tmem, m.bar);
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.A2, W, m.Bf + a.f_off[2], W, W + 16);
+      tc::mma_commit(m.bar);
+    }
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     tc::ld_32x32b_x32(trow, v);
     tc::ld_wait();
 #pragma unroll
     for (int i = 0; i < W; ++i) v[i] += m.bias[a.f_bias[2] + i];
-    put_row<BF16>(m.K, W, m.RH + t * SH, t, v, W);
+    put_row(m.HP, FH, t, v, W);
     {
       const float4* pf = reinterpret_cast<const float4*>(a.pe_feat + (long long)ray * PE_PAD);
-      float pe[32];
 #pragma unroll
       for (int k = 0; k < PE_PAD / 4; ++k) {
         const float4 x = __ldg(pf + k);
-        pe[4 * k] = x.x;
-        pe[4 * k + 1] = x.y;
-        pe[4 * k + 2] = x.z;
-        pe[4 * k + 3] = x.w;
+        v[4 * k] = x.x;
+        v[4 * k + 1] = x.y;
+        v[4 * k + 2] = x.z;
+        v[4 * k + 3] = x.w;
       }
-      pe[28] = pe[29] = pe[30] = pe[31] = 0.f;
-      put_row<BF16>(nullptr, 0, m.RH + t * SH, t, pe, 32, W);
+      v[28] = v[29] = v[30] = v[31] = 0.f;
+      put_row(m.HP, FH, t, v, 32, W);
     }
     sync_mma();
-    // layer 3 (mlp2 first, hidden part): relu(hid W3a^T + per-ray bias/PE) -> R4
-    issue<BF16>(m.Bf + a.f_off[3], a.f_K[3], a.f_N[3], m.K, tmem, m.bar);
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.HP, FH, m.Bf + a.f_off[3], W, W);  // hidden columns only (K = W)
+      tc::mma_commit(m.bar);
+    }
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     tc::ld_32x32b_x32(trow, v);
@@ -343,10 +297,13 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
         v[i + 3] = fmaxf(v[i + 3] + x.w, 0.f);
       }
     }
-    put_row<BF16>(m.K, W, m.R4 + t * W, t, v, W);
+    put_row(m.A4, W, t, v, W);
     sync_mma();
-    // layer 4: logits -> sigmoid -> delta4 = dL/dc * c (1 - c)
-    issue<BF16>(m.Bf + a.f_off[4], a.f_K[4], a.f_N[4], m.K, tmem, m.bar);
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.A4, W, m.Bf + a.f_off[4], W, 16);
+      tc::mma_commit(m.bar);
+    }
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     const float4 g = valid ? a.d4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -362,77 +319,88 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
       v[0] = g.y * c0 * (1.f - c0);
       v[1] = g.z * c1 * (1.f - c1);
       v[2] = g.w * c2 * (1.f - c2);
-      put_row<BF16>(m.K, 16, m.D + t * SD, t, v, 16);
+      put_row(m.D, FD, t, v, 16);
     }
     sync_mma();
-    // ---- backward ----
-    // through layer 4 (K = 16): dL/d relu(h3) = delta4 W4 ; delta3 = mask(R4) * that
-    issue<BF16>(m.Bb + a.b_off_img[4], a.b_K[4], a.b_N[4], m.K, tmem, m.bar);
-    accumulate<4, BF16>(acc, m.R4, W, m.D);
+    // ---- backward: per layer, delta propagation + weight-gradient MMA ----
+    // layer 4 (delta K = 16)
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.D, FD, m.Bb + a.b_off_img[4], 16, W);
+      mma_dw(tmem + DWCOL(4), m.D, m.A4, W, NIN(4), !first);
+      tc::mma_commit(m.bar);
+    }
+    if (t < OUT(4)) bias_acc[4] += column_sum(m.D, t);
+    ok = __syncthreads_and(wait_mma(m.bar, phase));
+    if (!ok) break;
+    tc::ld_32x32b_x32(trow, v);
+    tc::ld_wait();
+    relu_mask(m.A4, W, t, v, W);
+    put_row(m.D, FD, t, v, W);  // delta3
+    sync_mma();
+    // layer 3 (mlp2 first; delta K = W): d hidden; weight gradient over (hidden | PE)
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.D, FD, m.Bb + a.b_off_img[3], W, W);
+      mma_dw(tmem + DWCOL(3), m.D, m.HP, FH, NIN(3), !first);
+      tc::mma_commit(m.bar);
+    }
+    if (t < OUT(3)) bias_acc[3] += column_sum(m.D, t);
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
     {
-      float r[W];
-      get_row<BF16>(m.R4 + t * W, r, W);
-      tc::ld_32x32b_x32(trow, v);
-      tc::ld_wait();
-#pragma unroll
-      for (int i = 0; i < W; ++i) v[i] = (r[i] > 0.f) ? v[i] : 0.f;
-      put_row<BF16>(m.K, W, m.D + t * SD, t, v, W);
-    }
-    sync_mma();
-    // through layer 3 (K = W): d hidden = delta3 W3a ; delta of layer 2 = (dsigma, d hidden)
-    issue<BF16>(m.Bb + a.b_off_img[3], a.b_K[3], a.b_N[3], m.K, tmem, m.bar);
-    accumulate<3, BF16>(acc, m.RH, SH, m.D);
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    {
-      float dh[W];
+      float dh[32];
       tc::ld_32x32b_x32(trow, dh);
       tc::ld_wait();
       v[0] = g.x;
 #pragma unroll
       for (int i = 0; i < W; ++i) v[1 + i] = dh[i];
 #pragma unroll
-      for (int i = W + 1; i < KK; ++i) v[i] = 0.f;
-      put_row<BF16>(m.K, KK, m.D + t * SD, t, v, KK);
+      for (int i = W + 1; i < 48; ++i) v[i] = 0.f;
+      put_row(m.D, FD, t, v, 48);  // delta of layer 2: (dsigma, d hidden)
     }
     sync_mma();
-    // through layer 2 (K = W+16): delta1 = mask(R2) * (delta2 W2)
-    issue<BF16>(m.Bb + a.b_off_img[2], a.b_K[2], a.b_N[2], m.K, tmem, m.bar);
-    accumulate<2, BF16>(acc, m.R2, W, m.D);
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    {
-      float r[W];
-      get_row<BF16>(m.R2 + t * W, r, W);
-      tc::ld_32x32b_x32(trow, v);
-      tc::ld_wait();
-#pragma unroll
-      for (int i = 0; i < W; ++i) v[i] = (r[i] > 0.f) ? v[i] : 0.f;
-      put_row<BF16>(m.K, W, m.D + t * SD, t, v, W);
+    // layer 2 (mlp1 output; delta K = W + 16)
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.D, FD, m.Bb + a.b_off_img[2], W + 16, W);
+      mma_dw(tmem + DWCOL(2), m.D, m.A2, W, NIN(2), !first);
+      tc::mma_commit(m.bar);
     }
-    sync_mma();
-    // through layer 1: delta0 = mask(R1) * (delta1 W1)
-    issue<BF16>(m.Bb + a.b_off_img[1], a.b_K[1], a.b_N[1], m.K, tmem, m.bar);
-    accumulate<1, BF16>(acc, m.R1, W, m.D);
+    if (t < OUT(2)) bias_acc[2] += column_sum(m.D, t);
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
-    {
-      float r[W];
-      get_row<BF16>(m.R1 + t * W, r, W);
-      tc::ld_32x32b_x32(trow, v);
-      tc::ld_wait();
-#pragma unroll
-      for (int i = 0; i < W; ++i) v[i] = (r[i] > 0.f) ? v[i] : 0.f;
-      put_row<BF16>(m.K, W, m.D + t * SD, t, v, W);
+    tc::ld_32x32b_x32(trow, v);
+    tc::ld_wait();
+    relu_mask(m.A2, W, t, v, W);
+    put_row(m.D, FD, t, v, W);  // delta1
+    sync_mma();
+    // layer 1
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.D, FD, m.Bb + a.b_off_img[1], W, W);
+      mma_dw(tmem + DWCOL(1), m.D, m.A1, W, NIN(1), !first);
+      tc::mma_commit(m.bar);
     }
-    sync_mma();
-    // through layer 0: dL/dfeature = delta0 W0 (FP32) -> staging (aliases R1..)
-    issue<BF16>(m.Bb + a.b_off_img[0], a.b_K[0], a.b_N[0], m.K, tmem, m.bar);
-    accumulate<0, BF16>(acc, m.R0, C, m.D);
+    if (t < OUT(1)) bias_acc[1] += column_sum(m.D, t);
     ok = __syncthreads_and(wait_mma(m.bar, phase));
     if (!ok) break;
+    tc::ld_32x32b_x32(trow, v);
+    tc::ld_wait();
+    relu_mask(m.A1, W, t, v, W);
+    put_row(m.D, FD, t, v, W);  // delta0
+    sync_mma();
+    // layer 0: dL/dfeature (FP32) -> staging (aliases A1..HP, no longer read)
+    if (t == 0) {
+      tc::fence_after_sync();
+      mma_rows(tmem, m.D, FD, m.Bb + a.b_off_img[0], W, C);
+      mma_dw(tmem + DWCOL(0), m.D, m.X0, C, NIN(0), !first);
+      tc::mma_commit(m.bar);
+    }
+    if (t < OUT(0)) bias_acc[0] += column_sum(m.D, t);
+    ok = __syncthreads_and(wait_mma(m.bar, phase));
+    if (!ok) break;
+    first = false;
     {
       tc::ld_32x32b_x32(trow, v);
       tc::ld_wait();
@@ -460,45 +428,38 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
         }
       }
     }
-    __syncthreads();  // the next gather overwrites R0 / K; staging aliases R1..
+    tc::fence_before_sync();
+    __syncthreads();  // the next gather overwrites X0; staging aliases A1..HP
+    tc::fence_after_sync();
   }
   if (!ok && t == 0 && a.err) atomicExch(a.err, 1);
-  // ---- flush this CTA's weight gradient (packed torch layout) ----
+  // ---- flush: weight gradients from TMEM (row o = out index = this thread's lane) ----
+  if (ok && !first) {
 #pragma unroll
-  for (int k = 0; k < SLOTS; ++k) {
-    const int c = t + 128 * k;
-    if (c >= CHN) continue;
-    int L = 0;
+    for (int l = 0; l < NL; ++l) {
+      const int o = t;
 #pragma unroll
-    for (int l = 1; l < NL; ++l)
-      if (c >= BEGIN(l)) L = l;
-    const int local = c - BEGIN(L);
-    const int p = local / Q(L), jq = local - p * Q(L);
-    float* dst;
-    if (2 * p == INP(L)) {
-      dst = a.grad_params + a.b_off[L] + 4 * jq;
+      for (int c0 = 0; c0 < NIN(l); c0 += 32) {
+        tc::ld_32x32b_x32(tmem + lane + DWCOL(l) + c0, v);
+        tc::ld_wait();
+        if (o < OUT(l)) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) atomicAdd(dst + j, acc[k][j]);
-    } else {
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        const int i = 2 * p + r;
-        if (i >= IN(L)) continue;
-        dst = a.grad_params + a.w_off[L] + i * OUT4(L) + 4 * jq;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) atomicAdd(dst + j, acc[k][4 * r + j]);
+          for (int i = 0; i < 32; ++i)
+            if (c0 + i < IN(l)) atomicAdd(a.grad_params + a.w_off[l] + (c0 + i) * OUT4(l) + o, v[i]);
+        }
       }
+      if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, bias_acc[l]);
     }
   }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
 }
 
 inline size_t smem_bytes(const Args& a) {
-  return (size_t)a.wf_bytes + a.wb_bytes + a.nbias * 4 + 128 * KK * 2 + 128 * C * 2 + 2 * 128 * W * 2 +
-         128 * SH * 2 + 128 * W * 2 + 128 * SD * 2 + 16;
+  return (size_t)a.wf_bytes + a.wb_bytes + a.nbias * 4 + 128 * C * 2 + 2 * 128 * W * 2 + 128 * FH * 2 +
+         128 * W * 2 + 128 * FD * 2 + 16;
 }
 
 }  // namespace bw
@@ -511,7 +472,7 @@ static int resident_bwd(const void* kernel, size_t dyn_smem) {
   cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
   const int n = std::min({16, regs_sm / (std::max(fa.numRegs, 1) * 128),
-                          (int)(smem_sm / (dyn_smem + fa.sharedSizeBytes + 1024)), 512 / 64});
+                          (int)(smem_sm / (dyn_smem + fa.sharedSizeBytes + 1024)), 512 / bw::TMEM_COLS});
   return std::max(n, 1);
 }
 
@@ -528,7 +489,7 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
                      float* grad_params, int* err, void* stream) {
   using namespace dv::bw;
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
-  DV_CHECK(kind == 32 && channels == 32 && n_layers == NL, DV_ERR_UNSUPPORTED);
+  DV_CHECK(kind == 32 && channels == 32 && n_layers == NL && bf16 == 1, DV_ERR_UNSUPPORTED);
   if (n_seg == 0) return DV_OK;
   DV_CHECK(wf && wb && bias && f_layers && b_layers && voxels && seg && seg_ray && pe_feat && pe_out && d4 &&
                grad_voxels && grad_params,
@@ -585,7 +546,7 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
     DV_CHECK(a.f_bias[l] + fN[l] <= nbias, DV_ERR_ARG);
   }
   const size_t smem = smem_bytes(a);
-  auto k = bf16 ? decode_bwd_tc_kernel<1> : decode_bwd_tc_kernel<0>;
+  auto k = decode_bwd_tc_kernel;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return DV_ERR_CUDA;
   int dev = 0, sms = 0;

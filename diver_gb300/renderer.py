@@ -71,13 +71,13 @@ class TcWeights:
         self.bf16 = bool(bf16)
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.bwd = None
-        if decoder.kind == "diver32" and decoder.channels == 32:
+        if decoder.kind == "diver32" and decoder.channels == 32 and bf16:
             wb, tb = pack_tc_bwd(decoder, bf16)
             self.bwd = (wb.to(device), tb.contiguous())
 
     def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st) -> bool:
-        """Tensor-core backward; False when this decoder has none (the caller
-        then runs the FP32 backward)."""
+        """Tensor-core backward (DIVeR32, BF16); False when this decoder / form
+        has none (the caller then runs the FP32 CUDA backward)."""
         if self.bwd is None:
             return False
         nx, ny, nz, c = _grid(voxels)

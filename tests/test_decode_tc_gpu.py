@@ -84,9 +84,9 @@ def test_tc_render_error_vs_fp64_oracle(form):
     assert err <= TOL_RGB[form], err
 
 
-# Stated tolerances for the tensor-core training form (BF16 / FP16 operands,
-# FP32 accumulation): gradients within these relative L2 errors of the FP32
-# backward, per tensor.
+# Stated tolerances for the tensor-core training forms: gradients within these
+# relative L2 errors of the FP32 backward, per tensor.  BF16: tcgen05 forward
+# and backward (FP32 accumulation); FP16: tcgen05 forward, FP32 backward.
 TOL_GRAD = {"bf16": 3e-2, "fp16": 5e-3}
 
 
@@ -128,10 +128,10 @@ def test_tc_backward_on_the_small_scene_runs_full_tiles():
     o, v = scenes.small_view("cuda")
     tgt = torch.rand(o.shape[0], 3, generator=torch.Generator().manual_seed(1)).cuda()
     out = {}
-    for form in ("fp32", "fp16"):
+    for form in ("fp32", "bf16"):
         field = DIVeRField.from_scene(sc, "cuda")
         rgb, reg = field(o, v, form=form)
         (torch.nn.functional.mse_loss(rgb, tgt) + 1e-5 * reg).backward()
         out[form] = (field.voxels.grad.clone(), field.params.grad.clone())
-    for a, b in zip(out["fp16"], out["fp32"]):
-        assert ((a - b).norm() / b.norm()).item() <= TOL_GRAD["fp16"]
+    for a, b in zip(out["bf16"], out["fp32"]):
+        assert ((a - b).norm() / b.norm()).item() <= TOL_GRAD["bf16"]
