@@ -19,6 +19,8 @@
 #include "mlp.cuh"
 #include "tc.cuh"
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 namespace dv {
@@ -33,6 +35,7 @@ struct TcLayer {
 
 struct TcArgs {
   const float* grid;
+  const uint16_t* grid16;  // optional BF16/FP16 copy of the grid (same layout); used when non-null
   int nvx, nvy, nvz;
   const float* seg;
   const int* seg_ray;
@@ -66,6 +69,59 @@ __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long s0, ui
     }
     uint2 v = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
     *reinterpret_cast<uint2*>(sA + tc::kmajor_offset(ls, 4 * q, C)) = v;
+  }
+}
+
+template <int BF16>
+__device__ __forceinline__ void unpack8(const uint4 w, float* f) {
+  const uint32_t x[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (BF16) {
+      f[2 * j] = __uint_as_float(x[j] << 16);
+      f[2 * j + 1] = __uint_as_float(x[j] & 0xffff0000u);
+    } else {
+      f[2 * j] = __half2float(__ushort_as_half((unsigned short)(x[j] & 0xffffu)));
+      f[2 * j + 1] = __half2float(__ushort_as_half((unsigned short)(x[j] >> 16)));
+    }
+  }
+}
+
+// Gather from the 16-bit copy of the grid: C/8 threads per segment, each
+// reading 16 bytes (8 channels) of every corner row; the integral is FP32.
+template <int C, int BF16>
+__device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long s0, uint8_t* sA) {
+  constexpr int TPS = C / 8;
+  constexpr int SPP = 128 / TPS;
+  const int t = threadIdx.x;
+#pragma unroll 1
+  for (int p = 0; p < TPS; ++p) {
+    const int ls = p * SPP + t / TPS;
+    const int q = t % TPS;
+    const long long s = s0 + ls;
+    float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (s < a.S) {
+      const float* sg = a.seg + s * 6;
+      const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
+                                           __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
+      uint4 w[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j)
+        w[j] = __ldg(reinterpret_cast<const uint4*>(a.grid16 + corner_row(sc, j, a.nvx, a.nvy) * C) + q);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float g[8];
+        unpack8<BF16>(w[j], g);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) f[k] = fmaf(sc.w[j], g[k], f[k]);
+      }
+    }
+    uint4 o;
+    o.x = tc::pack2<BF16>(f[0], f[1]);
+    o.y = tc::pack2<BF16>(f[2], f[3]);
+    o.z = tc::pack2<BF16>(f[4], f[5]);
+    o.w = tc::pack2<BF16>(f[6], f[7]);
+    *reinterpret_cast<uint4*>(sA + tc::kmajor_offset(ls, 8 * q, C)) = o;
   }
 }
 
@@ -142,7 +198,10 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     const long long s0 = tile * 128;
     const long long s = s0 + t;
     const bool valid = s < a.S;
-    gather_tile_lp<C, BF16>(a, s0, sA);
+    if (a.grid16)
+      gather_tile_16<C, BF16>(a, s0, sA);
+    else
+      gather_tile_lp<C, BF16>(a, s0, sA);
     sync_for_mma();
     float v[32];
     // mlp1 hidden layers: D = relu(A W^T + b)
@@ -268,8 +327,9 @@ using namespace dv;
 extern "C" {
 
 int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
-                     const int* layers, int n_layers, const float* voxels, int nvx, int nvy, int nvz, const float* seg,
-                     const int* seg_ray, long long n_seg, const float* pe_out, float* out4, int* err, void* stream) {
+                     const int* layers, int n_layers, const float* voxels, const void* voxels16, int nvx, int nvy,
+                     int nvz, const float* seg, const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
+                     int* err, void* stream) {
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
   const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
   DV_CHECK(d1 > 0 && n_layers == d1 + 3 && n_layers <= TC_MAX_LAYERS, DV_ERR_ARG);
@@ -278,8 +338,10 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
   DV_CHECK(wblob && bias && layers && voxels && seg && seg_ray && pe_out && out4, DV_ERR_ARG);
   DV_CHECK(wbytes > 0 && wbytes % 16 == 0 && nbias > 0 && nbias % 4 == 0, DV_ERR_ARG);
   DV_CHECK(((uintptr_t)wblob & 15) == 0 && ((uintptr_t)voxels & 15) == 0 && ((uintptr_t)out4 & 15) == 0, DV_ERR_ARG);
+  DV_CHECK(voxels16 == nullptr || ((uintptr_t)voxels16 & 15) == 0, DV_ERR_ARG);
   TcArgs a{};
   a.grid = voxels;
+  a.grid16 = reinterpret_cast<const uint16_t*>(voxels16);
   a.nvx = nvx;
   a.nvy = nvy;
   a.nvz = nvz;

@@ -88,16 +88,18 @@ class TcWeights:
                N.ptr(d4), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
         return True
 
-    def decode(self, kind, channels, voxels, seg, pe_out, out4, st):
+    def decode(self, kind, channels, voxels, seg, pe_out, out4, st, voxels16=None):
         nx, ny, nz, c = _grid(voxels)
         _timed("dv_decode_fwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
-               self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), nx, ny, nz,
+               self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), N.ptr(voxels16),
+               nx, ny, nz,
                N.ptr(seg.seg), N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(out4), N.ptr(self.err), st)
 
 
 class SegmentRender(Function):
     @staticmethod
-    def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None):
+    def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None,
+                voxels16: torch.Tensor | None = None):
         nx, ny, nz, c = _grid(voxels)
         _check_params(kind, c, params)
         N.need_cuda("dirs", dirs, torch.float32)
@@ -114,7 +116,7 @@ class SegmentRender(Function):
             _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                    S, N.ptr(pe_out), N.ptr(out4), st)
         else:
-            tc.decode(kind, c, voxels, seg, pe_out, out4, st)
+            tc.decode(kind, c, voxels, seg, pe_out, out4, st, voxels16)
         rgb = torch.empty(B, 3, device=dev)
         reg = torch.empty(B, device=dev)
         _timed("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), int(bool(white_back)), N.ptr(rgb), None,
@@ -140,16 +142,18 @@ class SegmentRender(Function):
         gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
         if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st):
-            return gv, gp, None, None, None, None, None
+            return gv, gp, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
-        return gv, gp, None, None, None, None, None
+        return gv, gp, None, None, None, None, None, None
 
 
-def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None):
-    """(rgb [B,3], sparsity term) for the CSR segments of B rays; `tc` selects
-    the tensor-core decoder for the forward (the backward is FP32)."""
-    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc)
+def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None,
+                    voxels16: torch.Tensor | None = None):
+    """(rgb [B,3], sparsity term) for the CSR segments of B rays.  `tc` selects
+    the tensor-core decoder; `voxels16` (inference) is a BF16/FP16 copy of the
+    grid the tensor-core forward reads its corner rows from."""
+    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16)
 
 
 class DIVeRField(torch.nn.Module):
@@ -196,9 +200,23 @@ class DIVeRField(torch.nn.Module):
                                    self.mask_scale)
         return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size)
 
+    def grid16(self, form: str) -> torch.Tensor | None:
+        """BF16/FP16 copy of the feature grid for tensor-core rendering (made
+        once per grid version; None for the FP32 form)."""
+        if form == "fp32":
+            return None
+        key = ("grid16", form, self.voxels._version)
+        if getattr(self, "_g16key", None) != key:
+            dt = torch.bfloat16 if form == "bf16" else torch.float16
+            self._g16 = self.voxels.detach().to(dt).contiguous()
+            self._g16key = key
+        return self._g16
+
     def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32"):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
-        form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder forward)."""
+        form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder).  Without
+        autograd the tensor-core forms read a 16-bit copy of the grid."""
         seg = self.segments(os.contiguous(), ds.contiguous())
+        g16 = self.grid16(form) if not torch.is_grad_enabled() else None
         return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back,
-                               self.tc_weights(form))
+                               self.tc_weights(form), g16)

@@ -207,11 +207,15 @@ DV_API int dv_decode_bwd(int kind, int channels, const float* params, const floa
  * in FP32.  wblob holds every layer's weight matrix [N][K] in the K-major
  * 8x8 core-matrix layout; `layers` is a HOST array of n_layers rows
  * (byte offset, K, N, bias offset); bias [nbias] floats.  err (device int,
- * optional) is set to 1 if a bounded wait for an MMA ran out.
+ * optional) is set to 1 if a bounded wait for an MMA ran out.  voxels16
+ * (optional, may be NULL): a copy of the grid in the operand format (BF16
+ * when bf16 = 1, else FP16), same layout; when given, the corner rows are read
+ * from it (half the bytes) and integrated in FP32.
  */
 DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes,
                             const float* bias, int nbias, const int* layers, int n_layers,
-                            const float* voxels, int nvx, int nvy, int nvz, const float* seg,
+                            const float* voxels, const void* voxels16, int nvx, int nvy, int nvz,
+                            const float* seg,
                             const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
                             int* err, void* stream);
 

@@ -60,14 +60,16 @@ def test_tc_segments_match_fp32(kind, channels, form):
     N.call("dv_decode_fwd", k, channels, N.ptr(field.params), N.ptr(field.voxels), 65, 65, 65, N.ptr(seg.seg),
            N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(ref), st)
     tcw = field.tc_weights(form)
-    got = torch.empty_like(ref)
-    tcw.decode(k, channels, field.voxels, seg, pe_out, got, st)
-    torch.cuda.synchronize()
-    assert int(tcw.err.item()) == 0
-    err = (got - ref).abs().max(0).values.cpu().numpy()
     scale = ref.abs().max(0).values.cpu().numpy()
-    assert err[0] <= TOL_SEG[form] * max(1.0, scale[0]), (err, scale)
-    assert err[1:].max() <= TOL_SEG[form], (err, scale)
+    # FP32 grid rows, then the 16-bit copy of the grid used for rendering
+    for g16 in (None, field.grid16(form)):
+        got = torch.empty_like(ref)
+        tcw.decode(k, channels, field.voxels, seg, pe_out, got, st, g16)
+        torch.cuda.synchronize()
+        assert int(tcw.err.item()) == 0
+        err = (got - ref).abs().max(0).values.cpu().numpy()
+        assert err[0] <= TOL_SEG[form] * max(1.0, scale[0]), (err, scale, g16 is None)
+        assert err[1:].max() <= TOL_SEG[form], (err, scale, g16 is None)
 
 
 @pytest.mark.parametrize("form", ["bf16", "fp16"])
