@@ -274,7 +274,7 @@ def run_ours(args, rank, world, local):
     render = None
     if not args.no_render:
         render = {"resolution": [800, 800], "forms": {}}
-        with torch.no_grad():
+        with torch.no_grad(), Clocks(local) as rclk:
             for form in ("fp32", "bf16", "fp16"):
                 times = []
                 for k in range(2 + args.frames):
@@ -294,6 +294,7 @@ def run_ours(args, rank, world, local):
                                          "frames": len(times)}
         f = render["forms"]
         render["bf16_speedup_vs_fp32"] = f["bf16"]["Mrays_per_s"] / f["fp32"]["Mrays_per_s"]
+        render["clocks"] = rclk.summary()
     # ---- serving: 4 resident scenes, Poisson arrivals at 200 req/s ----
     serving = None
     if not args.no_serving and world == 1:

@@ -41,7 +41,8 @@ def main():
                 e0 = ev()
                 seg = field.segments(o, d)
                 e1 = ev()
-                R.render_segments(field.voxels, field.params, seg, d, kind, True, field.tc_weights(form))
+                R.render_segments(field.voxels, field.params, seg, d, kind, True, field.tc_weights(form),
+                                  field.grid16(form))
                 e2 = ev()
                 torch.cuda.synchronize()
                 k = {n: round(sum(s.elapsed_time(e) for s, e in v), 3) for n, v in R.KERNEL_EVENTS.items()}
