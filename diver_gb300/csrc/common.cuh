@@ -28,6 +28,44 @@ __device__ __forceinline__ float clampf(float v, float lo, float hi) {
   return fmaxf(lo, fminf(v, hi));
 }
 
+// Slab test against the box [0, n.x] x [0, n.y] x [0, n.z] (per-axis extents;
+// with n.x = n.y = n.z the arithmetic is exactly the cubic test below).
+__device__ __forceinline__ bool box_entry3(float3& p, const float3 d, const float3 n, float& t) {
+  const bool inside = (p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) &
+                      (p.x <= n.x) & (p.y <= n.y) & (p.z <= n.z);
+  if (inside) {
+    t = 0.f;
+    return true;
+  }
+  float a = __fdiv_rn(-p.x, d.x), b = __fdiv_rn(__fsub_rn(n.x, p.x), d.x);
+  float lo = fminf(a, b), hi = fmaxf(a, b);
+  a = __fdiv_rn(-p.y, d.y);
+  b = __fdiv_rn(__fsub_rn(n.y, p.y), d.y);
+  lo = fmaxf(lo, fminf(a, b));
+  hi = fminf(hi, fmaxf(a, b));
+  a = __fdiv_rn(-p.z, d.z);
+  b = __fdiv_rn(__fsub_rn(n.z, p.z), d.z);
+  lo = fmaxf(lo, fminf(a, b));
+  hi = fminf(hi, fmaxf(a, b));
+  p.x = clampf(__fmaf_rn(d.x, lo, p.x), 0.f, n.x);
+  p.y = clampf(__fmaf_rn(d.y, lo, p.y), 0.f, n.y);
+  p.z = clampf(__fmaf_rn(d.z, lo, p.z), 0.f, n.z);
+  t = lo;
+  return !(lo > hi);
+}
+
+__device__ __forceinline__ bool outside_closed3(const float3 b, const float3 n) {
+  return (b.x < 0.f) | (b.y < 0.f) | (b.z < 0.f) | (b.x > n.x) | (b.y > n.y) | (b.z > n.z);
+}
+
+// Linear occupancy index on an mx x my x mz grid (x fastest).
+__device__ __forceinline__ long long cell_index3(const float3 a, const float3 b, float scale, int mx, int my) {
+  const float cx = __fmul_rn(fminf(__fadd_rn(a.x, 1e-4f), __fadd_rn(b.x, 1e-4f)), scale);
+  const float cy = __fmul_rn(fminf(__fadd_rn(a.y, 1e-4f), __fadd_rn(b.y, 1e-4f)), scale);
+  const float cz = __fmul_rn(fminf(__fadd_rn(a.z, 1e-4f), __fadd_rn(b.z, 1e-4f)), scale);
+  return ((long long)(int)cz * my + (int)cy) * mx + (int)cx;
+}
+
 // Slab test of the ray (p, d) against the box [0, n]^3 in voxel units.
 // When p lies inside the box it is kept and t = 0.  Otherwise p becomes the
 // clamped point p + d*tmin and t = tmin.  Returns false on a miss (tmin > tmax);

@@ -21,6 +21,9 @@ struct WalkArgs {
   int max_n;
   float xyzmin;
   float n;
+  float3 o3;        // per-axis grid origin (world)
+  float3 n3;        // per-axis extent in voxels
+  int mx, my;       // occupancy cells along x and y (masked walk)
   float voxel_size;
   float mask_scale;
   int m;            // occupancy cells per side
@@ -48,6 +51,12 @@ __device__ __forceinline__ float3 ray_origin_voxel(const float* o, int b, float 
   return make_float3(__fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 0), xyzmin), vs),
                      __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 1), xyzmin), vs),
                      __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 2), xyzmin), vs));
+}
+
+__device__ __forceinline__ float3 ray_origin_voxel3(const float* o, int b, float3 o3, float vs) {
+  return make_float3(__fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 0), o3.x), vs),
+                     __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 1), o3.y), vs),
+                     __fdiv_rn(__fsub_rn(__ldg(o + 3 * b + 2), o3.z), vs));
 }
 
 __device__ __forceinline__ float3 load3(const float* p, int b) {
@@ -132,9 +141,9 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
   int count = 0;
   if (live) {
     const float3 d = load3(a.v, b);
-    float3 p = ray_origin_voxel(a.o, b, a.xyzmin, a.voxel_size);
+    float3 p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
     float t;
-    if (box_entry(p, d, a.n, t)) {
+    if (box_entry3(p, d, a.n3, t)) {
       const float3 s = signs(d);
       float* row = nullptr;
       float* trow = nullptr;
@@ -152,8 +161,8 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
       while (true) {
         grid_step(p, d, s, q, dt);
         t = __fadd_rn(t, dt);
-        if (outside_closed(q, a.n)) break;
-        const long long idx = cell_index(p, q, a.mask_scale, a.m);
+        if (outside_closed3(q, a.n3)) break;
+        const long long idx = cell_index3(p, q, a.mask_scale, a.mx, a.my);
         if (occupied(a.mask, idx, a.cells)) {
           if (MODE == WALK_PADDED && count < a.max_n) {
             float* r = row + 6 * count;
@@ -380,9 +389,12 @@ static WalkArgs walk_args(int batch, float xyzmin, float n, float vs, float mask
   a.batch = batch;
   a.xyzmin = xyzmin;
   a.n = n;
+  a.o3 = make_float3(xyzmin, xyzmin, xyzmin);
+  a.n3 = make_float3(n, n, n);
   a.voxel_size = vs;
   a.mask_scale = mask_scale;
   a.m = cells_per_side(n, mask_scale);
+  a.mx = a.my = a.m;
   a.cells = (long long)a.m * a.m * a.m;
   a.o = o;
   a.v = v;
@@ -495,6 +507,54 @@ int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* seg_coun
   if (batch_size == 0) return DV_OK;
   DV_CHECK(intersect_num && seg_count, DV_ERR_ARG);
   pair_counts_kernel<<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(batch_size, intersect_num, seg_count);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+// Per-axis grids: origin xyzmin[3] (world), extents dims[3] = (nx, ny, nz)
+// voxels, occupancy [nz][ny][nx] bytes (mask scale 1).
+static WalkArgs walk_args_grid(int batch, const float* xyzmin, const int* dims, float vs, const float* o,
+                               const float* v, const uint8_t* mask) {
+  WalkArgs a{};
+  a.batch = batch;
+  a.o3 = make_float3(xyzmin[0], xyzmin[1], xyzmin[2]);
+  a.n3 = make_float3((float)dims[0], (float)dims[1], (float)dims[2]);
+  a.voxel_size = vs;
+  a.mask_scale = 1.f;
+  a.mx = dims[0];
+  a.my = dims[1];
+  a.cells = (long long)dims[0] * dims[1] * dims[2];
+  a.o = o;
+  a.v = v;
+  a.mask = mask;
+  return a;
+}
+
+int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size, const float* o,
+                         const float* v, const uint8_t* mask, int* intersect_num, int* max_count, void* stream) {
+  DV_CHECK(batch_size >= 0 && xyzmin && dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && intersect_num, DV_ERR_ARG);
+  WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
+  a.num = intersect_num;
+  a.max_count = max_count;
+  masked_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size, const float* o,
+                            const float* v, const uint8_t* mask, const int64_t* offsets, float* seg, float* seg_t,
+                            int* seg_ray, void* stream) {
+  DV_CHECK(batch_size >= 0 && xyzmin && dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
+  WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
+  a.offsets = offsets;
+  a.seg = seg;
+  a.seg_t = seg_t;
+  a.seg_ray = seg_ray;
+  masked_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

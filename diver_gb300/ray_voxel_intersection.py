@@ -191,3 +191,34 @@ def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
         N.call("dv_dense_segments", B, float(xyzmin), float(voxel_num), float(voxel_size),
                N.ptr(o), N.ptr(v), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
     return Segments(offsets, seg, t, ray, pairs, M)
+
+
+def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask) -> Segments:
+    """Occupied-voxel segments over a grid with per-axis extents: xyzmin = world
+    position of corner (0,0,0) per axis, dims = (nx, ny, nz) voxels, mask
+    [nz][ny][nx].  The reference supports cubic grids only; with equal values on
+    the three axes this is exactly masked_segments with mask_scale 1."""
+    B = _check_rays(o, v)
+    nx, ny, nz = (int(x) for x in dims)
+    N.need_cuda("mask", mask)
+    if mask.numel() != nx * ny * nz:
+        raise ValueError(f"mask must hold {nz}x{ny}x{nx} cells, got {tuple(mask.shape)}")
+    m8 = mask.view(torch.uint8) if mask.dtype == torch.bool else mask
+    import ctypes
+
+    x0 = (ctypes.c_float * 3)(*[float(x) for x in xyzmin])
+    dd = (ctypes.c_int * 3)(nx, ny, nz)
+    dev = o.device
+    st = N.stream(dev)
+    num = torch.empty(B, dtype=torch.int32, device=dev)
+    N.call("dv_masked_count_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o), N.ptr(v),
+           N.ptr(m8), N.ptr(num), None, st)
+    offsets = exclusive_scan(num)
+    S, M = _totals(offsets, num)
+    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
+    t = torch.empty(S, dtype=torch.float32, device=dev)
+    ray = torch.empty(S, dtype=torch.int32, device=dev)
+    if S > 0:
+        N.call("dv_masked_segments_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o),
+               N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
+    return Segments(offsets, seg, t, ray, num, M)

@@ -21,7 +21,7 @@ from torch.autograd import Function
 
 from . import _native as N
 from .decoder import Decoder, pack_plain, pack_tc, pack_tc_bwd
-from .ray_voxel_intersection import Segments, dense_segments, masked_segments
+from .ray_voxel_intersection import Segments, dense_segments, masked_segments, masked_segments_grid
 
 KIND_ID = {"diver32": 32, "diver64": 64}
 WIDTH = {32: 32, 64: 64}
@@ -160,7 +160,7 @@ class DIVeRField(torch.nn.Module):
     """Explicit-grid DIVeR on the CUDA path: voxels [N+1]^3 x C and a packed
     decoder as parameters, an occupancy mask as a buffer."""
 
-    def __init__(self, voxels: torch.Tensor, decoder: Decoder, mask: torch.Tensor | None, xyzmin: float,
+    def __init__(self, voxels: torch.Tensor, decoder: Decoder, mask: torch.Tensor | None, xyzmin,
                  voxel_size: float, mask_scale: float = 1.0, white_back: bool = True):
         super().__init__()
         self.voxels = torch.nn.Parameter(voxels.contiguous())
@@ -168,7 +168,9 @@ class DIVeRField(torch.nn.Module):
         self.register_buffer("voxel_mask", None if mask is None else mask.contiguous())
         self.kind = decoder.kind
         self.voxel_num = voxels.shape[0] - 1
-        self.xyzmin = float(xyzmin)
+        self.dims = (voxels.shape[2] - 1, voxels.shape[1] - 1, voxels.shape[0] - 1)  # (nx, ny, nz)
+        self.aniso = isinstance(xyzmin, (tuple, list)) or len(set(self.dims)) > 1
+        self.xyzmin = tuple(float(x) for x in xyzmin) if isinstance(xyzmin, (tuple, list)) else float(xyzmin)
         self.voxel_size = float(voxel_size)
         self.mask_scale = float(mask_scale)
         self.white_back = white_back
@@ -195,6 +197,9 @@ class DIVeRField(torch.nn.Module):
                           scene.voxel_size, scene.mask_scale, scene.white_back)
 
     def segments(self, os: torch.Tensor, ds: torch.Tensor) -> Segments:
+        if self.aniso:
+            x0 = self.xyzmin if isinstance(self.xyzmin, tuple) else (self.xyzmin,) * 3
+            return masked_segments_grid(os, ds, x0, self.dims, self.voxel_size, self.voxel_mask)
         if self.voxel_mask is not None:
             return masked_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, self.voxel_mask,
                                    self.mask_scale)

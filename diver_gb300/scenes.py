@@ -30,7 +30,7 @@ class Scene:
     name: str
     voxel_num: int
     channels: int
-    xyzmin: float
+    xyzmin: float | tuple
     voxel_size: float
     features: torch.Tensor  # [N+1, N+1, N+1, C] float32, [z][y][x][c]
     mask: torch.Tensor  # [M, M, M] bool, [z][y][x]
@@ -40,7 +40,11 @@ class Scene:
 
     @property
     def xyzmax(self) -> float:
-        return self.xyzmin + self.voxel_num * self.voxel_size
+        return self.xyzmin + self.voxel_num * self.voxel_size if not isinstance(self.xyzmin, tuple) else None
+
+    @property
+    def dims(self):
+        return (self.features.shape[2] - 1, self.features.shape[1] - 1, self.features.shape[0] - 1)
 
     def to(self, device) -> "Scene":
         return Scene(self.name, self.voxel_num, self.channels, self.xyzmin, self.voxel_size,
@@ -169,6 +173,56 @@ def grid_scene(n=256, channels=32, kind="diver32", device="cpu", seed_offset: in
                  features(n + 1, channels, std, 0 + s, device),
                  blob_mask(n, xyzmin, vs, 16, 1 + s, device, occupancy),
                  1.0, random_decoder(kind, channels, 2 + s).to(device))
+
+
+def ellipsoid_mask(dims, xyzmin, vs, count, seed, device, occupancy=0.25):
+    """Union of `count` axis-aligned ellipsoids (centres in the box, semi-axes
+    U(0.05, 0.5)), uniformly rescaled so ~`occupancy` of the voxels are set."""
+    nx, ny, nz = dims
+    g = _gen(seed, "cpu")
+    lo = torch.tensor(xyzmin)
+    hi = lo + torch.tensor([nx, ny, nz], dtype=torch.float32) * vs
+    centres = lo + torch.rand(count, 3, generator=g) * (hi - lo)
+    axes = 0.05 + torch.rand(count, 3, generator=g) * 0.45
+    cx = xyzmin[0] + (torch.arange(nx, device=device) + 0.5) * vs
+    cy = xyzmin[1] + (torch.arange(ny, device=device) + 0.5) * vs
+    cz = xyzmin[2] + (torch.arange(nz, device=device) + 0.5) * vs
+    z, y, x = torch.meshgrid(cz, cy, cx, indexing="ij")
+
+    def build(scale):
+        m = torch.zeros(nz, ny, nx, dtype=torch.bool, device=device)
+        for c, a in zip(centres.to(device), (axes * scale).to(device)):
+            m |= ((x - c[0]) / a[0]) ** 2 + ((y - c[1]) / a[1]) ** 2 + ((z - c[2]) / a[2]) ** 2 <= 1.0
+        return m
+
+    s_lo, s_hi = 0.2, 4.0
+    for _ in range(12):  # bisection on a common scale of the semi-axes
+        mid = 0.5 * (s_lo + s_hi)
+        if build(mid).float().mean().item() < occupancy:
+            s_lo = mid
+        else:
+            s_hi = mid
+    return build(0.5 * (s_lo + s_hi))
+
+
+def wide_scene(device="cpu", dims=(320, 320, 160), seed_offset: int = 0) -> Scene:
+    """bbox [-1,1] x [-1,1] x [-0.5,0.5], voxel 1/160, 24-ellipsoid occupancy (~25%), DIVeR32."""
+    nx, ny, nz = dims
+    vs = 1.0 / 160
+    xyzmin = (-1.0, -1.0, -0.5)
+    s = seed_offset
+    g = _gen(0 + s, device)
+    feats = torch.randn(nz + 1, ny + 1, nx + 1, 32, generator=g, device=device, dtype=torch.float32) * 0.02
+    return Scene("wide", nx, 32, xyzmin, vs, feats, ellipsoid_mask(dims, xyzmin, vs, 24, 1 + s, device), 1.0,
+                 random_decoder("diver32", 32, 2 + s).to(device))
+
+
+def ellipse_cameras(count=150, a=3.0, b=2.0, z=0.8) -> list[torch.Tensor]:
+    cams = []
+    for k in range(count):
+        th = 2 * math.pi * k / count
+        cams.append(look_at(torch.tensor([a * math.cos(th), b * math.sin(th), z])))
+    return cams
 
 
 def reference_octree(mask: torch.Tensor) -> torch.Tensor:

@@ -117,6 +117,22 @@ DV_API int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, floa
                       const float* o, const float* v, const int64_t* offsets, float* seg,
                       float* seg_t, int* seg_ray, void* stream);
 
+/*
+ * Masked walk over a grid with per-axis extents (no counterpart in the
+ * reference, whose grids are cubic: voxel_num is a scalar, model/diver.py:
+ * 20-30).  xyzmin[3] (HOST array) is the world position of voxel corner
+ * (0,0,0), dims[3] (HOST array) = (nx, ny, nz) voxels, mask [nz][ny][nx]
+ * bytes.  With equal values on the three axes the arithmetic is exactly that
+ * of dv_masked_count / dv_masked_segments (mask_scale 1).
+ */
+DV_API int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size,
+                                const float* o, const float* v, const uint8_t* mask, int* intersect_num,
+                                int* max_count, void* stream);
+DV_API int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size,
+                                   const float* o, const float* v, const uint8_t* mask,
+                                   const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
+                                   void* stream);
+
 /* Per-ray segment counts for the dense pairing: max(intersect_num - 1, 0). */
 DV_API int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* seg_count, void* stream);
 

@@ -250,3 +250,57 @@ void oracle_ray_march(int batch, float* coords, const float* v, const uint8_t* m
     }
   }
 }
+
+/* Masked walk over a grid with per-axis extents dims[3] (nx, ny, nz) and
+ * origin xyzmin[3]: the same walk as oracle_masked_walk with the box
+ * [0,nx]x[0,ny]x[0,nz], occupancy [nz][ny][nx], mask scale 1. */
+void oracle_masked_walk_grid(int batch, int max_n, const float* xyzmin, const int* dims, float vs, const float* o,
+                             const float* v, const uint8_t* mask, float* inter, int* num, float* tns) {
+  float nx = (float)dims[0], ny = (float)dims[1], nz = (float)dims[2];
+  long long cells = (long long)dims[0] * dims[1] * dims[2];
+  for (int b = 0; b < batch; ++b) {
+    v3 d = {v[3 * b], v[3 * b + 1], v[3 * b + 2]};
+    v3 p = {(o[3 * b] - xyzmin[0]) / vs, (o[3 * b + 1] - xyzmin[1]) / vs, (o[3 * b + 2] - xyzmin[2]) / vs};
+    float t = 0.f;
+    int count = 0, hit = 1;
+    int inside = (p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x <= nx) & (p.y <= ny) & (p.z <= nz);
+    if (!inside) {
+      float a = (-p.x) / d.x, c = (nx - p.x) / d.x;
+      float lo = fminf(a, c), hi = fmaxf(a, c);
+      a = (-p.y) / d.y; c = (ny - p.y) / d.y;
+      lo = fmaxf(lo, fminf(a, c)); hi = fminf(hi, fmaxf(a, c));
+      a = (-p.z) / d.z; c = (nz - p.z) / d.z;
+      lo = fmaxf(lo, fminf(a, c)); hi = fminf(hi, fmaxf(a, c));
+      p.x = clampf(fmaf(d.x, lo, p.x), 0.f, nx);
+      p.y = clampf(fmaf(d.y, lo, p.y), 0.f, ny);
+      p.z = clampf(fmaf(d.z, lo, p.z), 0.f, nz);
+      t = lo;
+      hit = !(lo > hi);
+    }
+    if (hit) {
+      v3 s = {sgnf(d.x), sgnf(d.y), sgnf(d.z)};
+      float* row = inter + (long long)b * max_n * 6;
+      float* trow = tns + (long long)b * max_n;
+      for (;;) {
+        float dt;
+        v3 q = grid_step(p, d, s, &dt, 1);
+        t = t + dt;
+        if ((q.x < 0.f) | (q.y < 0.f) | (q.z < 0.f) | (q.x > nx) | (q.y > ny) | (q.z > nz)) break;
+        float cx = fminf(p.x + 1e-4f, q.x + 1e-4f), cy = fminf(p.y + 1e-4f, q.y + 1e-4f),
+              cz = fminf(p.z + 1e-4f, q.z + 1e-4f);
+        long long idx = ((long long)(int)cz * dims[1] + (int)cy) * dims[0] + (int)cx;
+        if (occ(mask, idx, cells)) {
+          if (count < max_n) {
+            float* r = row + 6 * count;
+            r[0] = p.x; r[1] = p.y; r[2] = p.z;
+            r[3] = q.x; r[4] = q.y; r[5] = q.z;
+            trow[count] = t * vs;
+          }
+          ++count;
+        }
+        p = q;
+      }
+    }
+    num[b] = count;
+  }
+}

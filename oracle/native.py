@@ -20,6 +20,8 @@ def lib():
         h = C.CDLL(str(_build.build()))
         h.oracle_dense_walk.argtypes = [I, I, F, F, F, P, P, P, P, P, I]
         h.oracle_masked_walk.argtypes = [I, I, F, F, F, F, P, P, P, P, P, P, I]
+        h.oracle_masked_walk_grid.argtypes = [I, I, P, P, F, P, P, P, P, P, P]
+        h.oracle_masked_walk_grid.restype = None
         h.oracle_aabb.argtypes = [I, P, P, P, P, P, P, I, I]
         h.oracle_ray_march.argtypes = [I, P, P, P, P, I, I]
         for n in ("oracle_mlp_eval_f32", "oracle_mlp_eval_f64"):
@@ -62,6 +64,22 @@ def masked_walk(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, max_n=Non
     num = np.zeros(B, np.int32)
     lib().oracle_masked_walk(B, max_n, xyzmin, float(voxel_num), voxel_size, mask_scale, _p(o), _p(v), _p(m),
                              _p(inter), _p(num), _p(tns), int(fused))
+    return inter, num, tns
+
+
+def masked_walk_grid(o, v, xyzmin, dims, voxel_size, mask, max_n=None):
+    """Masked walk over a per-axis grid: xyzmin (3,), dims (nx, ny, nz), mask [nz][ny][nx]."""
+    o, v = _f32(o), _f32(v)
+    m = np.ascontiguousarray(np.asarray(mask).astype(np.uint8))
+    x0 = _f32(xyzmin)
+    dd = np.ascontiguousarray(np.asarray(dims, np.int32))
+    B = o.shape[0]
+    max_n = int(sum(dims)) if max_n is None else max_n
+    inter = np.zeros((B, max_n, 6), np.float32)
+    tns = np.full((B, max_n), -1.0, np.float32)
+    num = np.zeros(B, np.int32)
+    lib().oracle_masked_walk_grid(B, max_n, _p(x0), _p(dd), voxel_size, _p(o), _p(v), _p(m), _p(inter), _p(num),
+                                  _p(tns))
     return inter, num, tns
 
 

@@ -20,11 +20,18 @@ import math
 import torch
 
 
-def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor) -> torch.Tensor:
+def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor, per_axis: bool = False) -> torch.Tensor:
+    """per_axis: clamp each axis to its own vertex count (grids that are not
+    cubic); the reference clamps every axis with voxels.shape[-2]."""
     n, c = voxels.shape[-2:]
     pmin = torch.min((coord_i + 1e-4).long(), (coord_o + 1e-4).long())
     xmin, ymin, zmin = pmin.split(1, dim=-1)
-    xmax, ymax, zmax = (pmin + 1).clamp_max(n - 1).split(1, dim=-1)
+    if per_axis:
+        nz, ny, nx = voxels.shape[:3]
+        hi = torch.tensor([nx - 1, ny - 1, nz - 1])
+        xmax, ymax, zmax = torch.minimum(pmin + 1, hi).split(1, dim=-1)
+    else:
+        xmax, ymax, zmax = (pmin + 1).clamp_max(n - 1).split(1, dim=-1)
     corners = [voxels[zmin, ymin, xmin], voxels[zmin, ymin, xmax], voxels[zmin, ymax, xmin], voxels[zmin, ymax, xmax],
                voxels[zmax, ymin, xmin], voxels[zmax, ymin, xmax], voxels[zmax, ymax, xmin], voxels[zmax, ymax, xmax]]
     F = torch.stack(corners, 0).reshape(2, 2, 2, -1, c)  # [z][y][x]
@@ -91,9 +98,9 @@ def render(color: torch.Tensor, sigma: torch.Tensor, mask: torch.Tensor, white_b
     return rgb, weight
 
 
-def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True):
+def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True, per_axis=False):
     """Full decode path over CSR segments: returns rgb [B,3], sigma [B,M], mask [B,M]."""
-    feat = integrate(voxels, seg[:, :3], seg[:, 3:])
+    feat = integrate(voxels, seg[:, :3], seg[:, 3:], per_axis)
     s, c = decode(layers, n_mlp1, feat, dirs[seg_ray.long()])
     sigma, mask = scatter_padded(s, counts)
     color, _ = scatter_padded(c, counts)
