@@ -58,6 +58,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--requests", type=int, default=24)
+    p.add_argument("--no-extra", action="store_true", help="skip the wide-grid, 64-channel and real-time sections")
     p.add_argument("--form", default="bf16", choices=["fp32", "bf16", "fp16"],
                    help="decoder form of the headline training step (the FP32 form is always timed too)")
     return p.parse_args()
@@ -295,6 +296,13 @@ def run_ours(args, rank, world, local):
         f = render["forms"]
         render["bf16_speedup_vs_fp32"] = f["bf16"]["Mrays_per_s"] / f["fp32"]["Mrays_per_s"]
         render["clocks"] = rclk.summary()
+    extra = None
+    if not args.no_extra and world == 1:
+        del field, batches
+        torch.cuda.empty_cache()
+        extra = {"wide_train": run_wide_train(args, dev), "rt64_render": run_rt64_render(args, dev),
+                 "realtime_frame": run_realtime(args, dev)}
+        torch.cuda.empty_cache()
     # ---- serving: 4 resident scenes, Poisson arrivals at 200 req/s ----
     serving = None
     if not args.no_serving and world == 1:
@@ -328,6 +336,7 @@ def run_ours(args, rank, world, local):
         "gpu_launches": OUR_LAUNCHES_PER_STEP * args.steps,
         "roofline": roofline,
         "train_forms": train_forms,
+        "configs": extra,
         "render": render,
         "serving": serving,
         "segments_per_step": statistics.mean(seg_counts),
@@ -336,6 +345,109 @@ def run_ours(args, rank, world, local):
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(scene, batches[args.warmup], sample=256, repeats=3)
     return line
+
+
+def _time_steps(fn, warmup, steps):
+    import torch
+
+    for _ in range(warmup):
+        fn(0)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for i in range(steps):
+        fn(i)
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / steps
+
+
+def run_wide_train(args, dev):
+    """Wide grid 320x320x160 x 32 (bbox [-1,1]^2 x [-0.5,0.5], 24 ellipsoids ~25%),
+    150 cameras on an ellipse (a=3, b=2, z=0.8) at 1920x1080, batch 8192 rays
+    that hit occupied voxels; training fwd+bwd per form."""
+    import torch
+
+    from diver_gb300 import _native as N
+    from diver_gb300 import scenes
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.wide_scene(dev)
+    field = DIVeRField(sc.features, sc.decoder, sc.mask, sc.xyzmin, sc.voxel_size)
+    cams = scenes.ellipse_cameras(150)
+    dirs_cam = scenes.pixel_directions(1080, 1920, 1.2 * 1920, dev).reshape(-1, 3)
+    g = torch.Generator(device=dev).manual_seed(4)
+    gc = torch.Generator().manual_seed(4)
+    B = 8192
+    batches = []
+    while len(batches) < 8:
+        c2w = cams[int(torch.randint(0, 150, (1,), generator=gc))].to(dev)
+        pick = torch.randint(0, dirs_cam.shape[0], (4 * B,), generator=g, device=dev)
+        d = dirs_cam[pick] @ c2w[:, :3].t()
+        d = (d / d.norm(dim=-1, keepdim=True)).contiguous()
+        o = c2w[:, 3].expand(d.shape).contiguous()
+        seg = field.segments(o, d)
+        keep = torch.nonzero(seg.counts > 0)[:, 0]
+        if keep.numel() >= B:
+            keep = keep[:B]
+            batches.append((o[keep].contiguous(), d[keep].contiguous(), torch.rand(B, 3, generator=g, device=dev)))
+    out = {"grid": list(sc.dims), "occupancy": float(sc.mask.float().mean()), "batch": B}
+    for form in ("fp32", "bf16"):
+        ms = _time_steps(lambda i: train_step(field, *batches[i % 8], form=form), 2, 8)
+        out[form] = {"ms_per_step": ms, "Mrays_per_s": B / (ms * 1e-3) / 1e6}
+    out["bf16_speedup_vs_fp32"] = out["bf16"]["Mrays_per_s"] / out["fp32"]["Mrays_per_s"]
+    return out
+
+
+def run_rt64_render(args, dev):
+    """256^3 x 64-channel scene with a DIVeR64 decoder: full 800x800 frames from
+    spiral cameras (radius 4, elevation -30..30 deg) per decoder form."""
+    import torch
+
+    from diver_gb300 import scenes
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.grid_scene(256, 64, "diver64", device=dev)
+    field = DIVeRField.from_scene(sc, dev)
+    cams = scenes.spiral_cameras(200, 4.0)
+    rays = [scenes.camera_rays(cams[k * 40], 800, 800, 960.0, dev) for k in range(4)]
+    out = {}
+    with torch.no_grad():
+        for form in ("fp32", "bf16", "fp16"):
+            ms = _time_steps(lambda i: field(*rays[i % 4], form=form), 1, 4)
+            out[form] = {"frame_ms": ms, "Mrays_per_s": 640000 / (ms * 1e-3) / 1e6}
+    out["bf16_speedup_vs_fp32"] = out["bf16"]["Mrays_per_s"] / out["fp32"]["Mrays_per_s"]
+    return out
+
+
+def run_realtime(args, dev):
+    """Real-time path (eval_rt.py): the 256^3 x 32 scene converted to the serialized
+    form (sparse feature table of occupied voxels' corners), octree first hit, then
+    rounds of 8-hit march + fused decoder with early termination, 800x800."""
+    import torch
+
+    from diver_gb300 import scenes
+    from diver_gb300.realtime import RealtimeModel, convert
+
+    sc = scenes.grid_scene(256, 32, "diver32", device=dev)
+    sd = {"voxels": sc.features.cpu()}
+    sd.update({k: v.cpu() for k, v in sc.decoder.state_dict().items()})
+    ser = convert(sd, sc.mask.float().cpu())
+    model = RealtimeModel.from_serialized(ser, 256, sc.xyzmin, sc.voxel_size, dev)
+    cams = scenes.sphere_cameras(100, 4.0, 3)
+    frames = []
+    for k in range(3):
+        _, d = scenes.camera_rays(cams[k], 800, 800, 960.0, dev)
+        frames.append((cams[k][:, 3], d))
+    rounds = []
+
+    def frame(i):
+        _, r = model.render_frame(*frames[i % 3])
+        rounds.append(r)
+
+    ms = _time_steps(frame, 1, 3)
+    return {"frame_ms": ms, "Mrays_per_s": 640000 / (ms * 1e-3) / 1e6, "rounds": rounds[-1],
+            "features": int(ser["f"].shape[0])}
 
 
 def run_serving(args, dev):
