@@ -298,7 +298,7 @@ def run_ours(args, rank, world, local):
         render["clocks"] = rclk.summary()
     extra = None
     if not args.no_extra and world == 1:
-        del field, batches
+        del field
         torch.cuda.empty_cache()
         extra = {"wide_train": run_wide_train(args, dev), "rt64_render": run_rt64_render(args, dev),
                  "realtime_frame": run_realtime(args, dev)}
@@ -430,9 +430,9 @@ def run_realtime(args, dev):
     from diver_gb300.realtime import RealtimeModel, convert
 
     sc = scenes.grid_scene(256, 32, "diver32", device=dev)
-    sd = {"voxels": sc.features.cpu()}
-    sd.update({k: v.cpu() for k, v in sc.decoder.state_dict().items()})
-    ser = convert(sd, sc.mask.float().cpu())
+    sd = {"voxels": sc.features}
+    sd.update(sc.decoder.state_dict())
+    ser = convert(sd, sc.mask.float())
     model = RealtimeModel.from_serialized(ser, 256, sc.xyzmin, sc.voxel_size, dev)
     cams = scenes.sphere_cameras(100, 4.0, 3)
     frames = []

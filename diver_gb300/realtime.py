@@ -33,15 +33,17 @@ def convert(state_dict: dict, alpha_map: torch.Tensor, thresh: float = 1e-2) -> 
     kind = "diver32" if "mlp1.4.weight" in sd else "diver64"
     dec = Decoder.from_state_dict(kind, sd)
     voxels = sd["voxels"].float()
+    dev = voxels.device
+    voxel_mask = voxel_mask.to(dev)
     nv = voxels.shape[0]
     occ = torch.nonzero(voxel_mask)  # [K,3] (z, y, x) of occupied voxels
-    offs = torch.stack(torch.meshgrid(*[torch.arange(2)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    offs = torch.stack(torch.meshgrid(*[torch.arange(2, device=dev)] * 3, indexing="ij"), -1).reshape(-1, 3)
     idx = (occ[None] + offs[:, None]).reshape(-1, 3).unique(dim=0)  # sorted lexicographically
     feats = voxels[idx[:, 0], idx[:, 1], idx[:, 2]]
     feats = premultiply_features(dec, feats) if kind == "diver32" else feats.contiguous()
     n = nv - 1
     valid = (idx < n).all(1)
-    m = torch.zeros(idx.shape[0], dtype=torch.bool)
+    m = torch.zeros(idx.shape[0], dtype=torch.bool, device=dev)
     iv = idx[valid]
     m[valid] = voxel_mask[iv[:, 0], iv[:, 1], iv[:, 2]]
     inds = idx[:, 0] * nv * nv + idx[:, 1] * nv + idx[:, 2]
@@ -68,19 +70,19 @@ class RealtimeModel:
     def from_serialized(ser: dict, voxel_num: int, xyzmin: float, voxel_size: float, device="cuda",
                         width: int | None = None) -> "RealtimeModel":
         nv = voxel_num + 1
-        inds = ser["i"].long()
+        inds = ser["i"].to(device).long()
         ii, rem = inds // (nv * nv), inds % (nv * nv)
         jj, kk = rem // nv, rem % nv
-        masks = torch.zeros(voxel_num, voxel_num, voxel_num, dtype=torch.bool)
-        mm = ser["m"].bool()
+        masks = torch.zeros(voxel_num, voxel_num, voxel_num, dtype=torch.bool, device=device)
+        mm = ser["m"].to(device).bool()
         masks[ii[mm], jj[mm], kk[mm]] = True
-        vmap = torch.zeros(nv, nv, nv, dtype=torch.int32)
-        vmap[ii, jj, kk] = torch.arange(inds.numel(), dtype=torch.int32)
+        vmap = torch.zeros(nv, nv, nv, dtype=torch.int32, device=device)
+        vmap[ii, jj, kk] = torch.arange(inds.numel(), dtype=torch.int32, device=device)
         p = ser["p"]
         if width is None:
             width = 32 if p.numel() == 3168 else 64
-        masks = masks.to(device).contiguous()
-        return RealtimeModel(ser["f"].to(device).float().contiguous(), vmap.to(device).contiguous(), masks,
+        masks = masks.contiguous()
+        return RealtimeModel(ser["f"].to(device).float().contiguous(), vmap.contiguous(), masks,
                              build_octree_levels(masks), RealtimeModel.pack_params(p, width, device), width,
                              voxel_num, xyzmin, voxel_size)
 
