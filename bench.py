@@ -227,8 +227,11 @@ def run_ours(args, rank, world, local):
     scene = train_scene(dev)
     field = DIVeRField.from_scene(scene, dev)
     batches = make_batches(scene, args.warmup + args.steps, dev)
-    forms = {}
+    from diver_gb300.graphs import TrainStepGraph
+
+    forms, graphs = {}, {}
     for form in ("fp32", args.form) if args.form != "fp32" else ("fp32",):
+        # eager pipeline, with per-kernel CUDA events
         for i in range(args.warmup):
             train_step(field, *batches[i], form=form)
         torch.cuda.synchronize()
@@ -247,15 +250,41 @@ def run_ours(args, rank, world, local):
         kms = {k: [s.elapsed_time(e) for s, e in v] for k, v in R.KERNEL_EVENTS.items()}
         R.KERNEL_EVENTS = None
         forms[form] = (start.elapsed_time(end), kms, clk.summary())
+        # the same step captured once in a CUDA graph and replayed
+        step = TrainStepGraph(field, *batches[0], form=form, l_s=L_S)
+        for i in range(args.warmup):
+            step(*batches[i])
+        torch.cuda.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            start.record()
+            for i in range(args.steps):
+                step(*batches[args.warmup + i])
+            end.record()
+            torch.cuda.synchronize()
+        barrier(world)
+        graphs[form] = (start.elapsed_time(end), clk.summary())
+        if form != args.form:
+            del step
     tform = args.form
-    ms, kernel_ms, clocks = forms[tform]
+    ms, clocks = graphs[tform]
+    kernel_ms = forms[tform][1]
     # segments per step (for the roofline): recount with the same traversal
     seg_counts = [field.segments(*batches[args.warmup + i][:2]).total for i in range(args.steps)]
     ms_max = allreduce_max(ms, world)
     rays = allreduce_sum(float(BATCH * args.steps), world)
     value = rays / (ms_max * 1e-3) / 1e6
-    train_forms = {f: {"Mrays_per_s": rays / (allreduce_max(v[0], world) * 1e-3) / 1e6,
-                       "ms_per_step": v[0] / args.steps} for f, v in forms.items()}
+    train_forms = {}
+    for f in forms:
+        train_forms[f] = {"eager": {"Mrays_per_s": rays / (allreduce_max(forms[f][0], world) * 1e-3) / 1e6,
+                                    "ms_per_step": forms[f][0] / args.steps},
+                          "graph": {"Mrays_per_s": rays / (allreduce_max(graphs[f][0], world) * 1e-3) / 1e6,
+                                    "ms_per_step": graphs[f][0] / args.steps}}
+    if "fp32" in forms and tform != "fp32":
+        train_forms["speedup_vs_fp32"] = {m: train_forms[tform][m]["Mrays_per_s"] / train_forms["fp32"][m]["Mrays_per_s"]
+                                          for m in ("eager", "graph")}
     # ---- e2e: pinned host inputs, H2D + D2H inside the timed region ----
     host = [tuple(t.cpu().pin_memory() for t in b) for b in batches[args.warmup:]]
     torch.cuda.synchronize()
@@ -264,8 +293,7 @@ def run_ours(args, rank, world, local):
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record()
     for o_h, d_h, g_h in host:
-        o, d, tgt = (x.to(dev, non_blocking=True) for x in (o_h, d_h, g_h))
-        loss, _, _ = train_step(field, o, d, tgt, form=tform)
+        loss, _, _ = step(o_h, d_h, g_h)  # H2D copies into the graph's inputs, replay
         loss.item()
     t1.record()
     torch.cuda.synchronize()
@@ -298,7 +326,7 @@ def run_ours(args, rank, world, local):
         render["clocks"] = rclk.summary()
     extra = None
     if not args.no_extra and world == 1:
-        del field
+        del field, step
         torch.cuda.empty_cache()
         extra = {"wide_train": run_wide_train(args, dev), "rt64_render": run_rt64_render(args, dev),
                  "realtime_frame": run_realtime(args, dev)}
@@ -328,8 +356,9 @@ def run_ours(args, rank, world, local):
                 "targets U[0,1]",
         "config": {"workload": "train fwd+bwd, DIVeR32, 256^3 x 32 features, batch 4096 rays that hit occupied voxels",
                    "global_batch": BATCH * world,
-                   "form": "plain FP32" if tform == "fp32" else f"tcgen05 {tform.upper()} decoder fwd+bwd, FP32 accumulation, "
-                           "FP32 integration/compositing/weight-gradient accumulation",
+                   "form": ("plain FP32" if tform == "fp32" else f"tcgen05 {tform.upper()} decoder fwd+bwd, FP32 accumulation, "
+                            "FP32 integration/compositing/weight-gradient accumulation")
+                           + "; the whole step captured once in a CUDA graph and replayed (diver_gb300.graphs)",
                    "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (2.2 GB grid), a fresh batch every step"},
         "e2e": {"value": e2e_val, "unit": "Mrays/s", "h2d_bytes_per_step": BATCH * 9 * 4, "d2h_bytes_per_step": 4},

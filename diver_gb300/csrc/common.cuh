@@ -95,18 +95,55 @@ __device__ __forceinline__ bool box_entry(float3& p, const float3 d, const float
   return !(lo > hi);
 }
 
+// Quotient x / d rounded to nearest from r = RN(1/d):
+//   q = RN(x * r),  e = x - d * q (exact in one FMA),  result = RN(q + e * r).
+// By Markstein's theorem (P. W. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990) this is the correctly rounded quotient, the same bits as __fdiv_rn,
+// whenever no intermediate overflows or underflows.  The walks divide the
+// distance to the next grid plane (|x| between 2^-24 and 2 for points inside
+// a grid of fewer than 2^23 voxels per side) by a direction component, so
+// recip_ok() admits a direction only when every component has
+// 2^-60 <= |d| <= 2^60; other rays take the __fdiv_rn form of the step.
+__device__ __forceinline__ float div_by_recip(float x, float d, float r) {
+  const float q = __fmul_rn(x, r);
+  const float e = __fmaf_rn(-q, d, x);
+  return __fmaf_rn(e, r, q);
+}
+
+__device__ __forceinline__ bool recip_ok(const float3 d) {
+  const float lo = 8.67361738e-19f, hi = 1.15292150e18f;  // 2^-60, 2^60
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  return (ax >= lo) & (ax <= hi) & (ay >= lo) & (ay <= hi) & (az >= lo) & (az <= hi);
+}
+
+__device__ __forceinline__ float3 recip3(const float3 d) {
+  return make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+}
+
+template <bool FAST>
+__device__ __forceinline__ float step_div(float x, float d, float r) {
+  if constexpr (FAST) {
+    return div_by_recip(x, d, r);
+  } else {
+    return __fdiv_rn(x, d);
+  }
+}
+
 // One step of the 3D-DDA: from point a, move along d to the nearest grid
 // plane crossing b; dt is the parameter increment.  The coordinate of the
 // plane that was hit is snapped onto the plane, with ties resolved x, then y,
-// then z.  Reference: ray_voxel_intersect.cu:119-135.
-__device__ __forceinline__ void grid_step(const float3 a, const float3 d, const float3 s,
+// then z.  r = recip3(d) when FAST (unused otherwise).
+// Reference: ray_voxel_intersect.cu:119-135.
+template <bool FAST>
+__device__ __forceinline__ void grid_step(const float3 a, const float3 d, const float3 r, const float3 s,
                                           float3& b, float& dt) {
   const float bx = __fmul_rn(floorf(__fmaf_rn(a.x, s.x, 1.f)), s.x);
   const float by = __fmul_rn(floorf(__fmaf_rn(a.y, s.y, 1.f)), s.y);
   const float bz = __fmul_rn(floorf(__fmaf_rn(a.z, s.z, 1.f)), s.z);
-  const float tx = __fdiv_rn(__fsub_rn(bx, a.x), d.x);
-  const float ty = __fdiv_rn(__fsub_rn(by, a.y), d.y);
-  const float tz = __fdiv_rn(__fsub_rn(bz, a.z), d.z);
+  const float tx = step_div<FAST>(__fsub_rn(bx, a.x), d.x, r.x);
+  const float ty = step_div<FAST>(__fsub_rn(by, a.y), d.y, r.y);
+  const float tz = step_div<FAST>(__fsub_rn(bz, a.z), d.z, r.z);
   dt = fminf(tx, fminf(ty, tz));
   b.x = __fmaf_rn(d.x, dt, a.x);
   b.y = __fmaf_rn(d.y, dt, a.y);
@@ -153,6 +190,16 @@ __device__ __forceinline__ long long cell_index1(const float3 a, const float3 b,
 // along the far face) counts as empty instead of reading past the buffer.
 __device__ __forceinline__ bool occupied(const uint8_t* __restrict__ mask, long long idx, long long cells) {
   return (idx >= 0 && idx < cells) ? (__ldg(mask + idx) != 0) : false;
+}
+
+// Segment count of a decode launch: `cap` (the host count, or the capacity of
+// the segment buffers) or, when `dev` is given, the count the device holds
+// there (the CSR end offsets[B]) clamped to [0, cap].  Reading it on the
+// device lets a launch be recorded in a CUDA graph before the count exists.
+__device__ __forceinline__ long long segment_total(long long cap, const int64_t* dev) {
+  if (dev == nullptr) return cap;
+  const long long v = (long long)*dev;
+  return v < 0 ? 0 : (v < cap ? v : cap);
 }
 
 __host__ __device__ __forceinline__ unsigned ceil_div(long long a, long long b) {

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(256) composite_bwd_kernel(const DecodeArgs a, 
   const long long beg = a.offsets[ray], end = a.offsets[ray + 1];
   const float g0 = a.g_rgb[3 * ray], g1 = a.g_rgb[3 * ray + 1], g2 = a.g_rgb[3 * ray + 2];
   const float grgb = g0 * a.rgb[3 * ray] + g1 * a.rgb[3 * ray + 1] + g2 * a.rgb[3 * ray + 2];
+  const float rc = a.reg_scale ? a.reg_coef * *a.reg_scale : a.reg_coef;
   Kahan logt;
   float carry = 0.f;  // sum_{j < chunk} w_j (g . c_j)
   for (long long base = beg; base < end; base += 32) {
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(256) composite_bwd_kernel(const DecodeArgs a, 
     const float pincl = warp_incl_scan(w * gc) + carry;
     float ds = Tn * gc - grgb + pincl;
     float dsig = v.x > 0.f ? ds : 0.f;
-    dsig += a.reg_coef * 2.f * v.x / (0.5f + v.x * v.x);
+    dsig += rc * 2.f * v.x / (0.5f + v.x * v.x);
     if (valid) d4[i] = make_float4(dsig, w * g0, w * g1, w * g2);
     logt.add(__shfl_sync(0xffffffffu, incl, 31));
     carry = __shfl_sync(0xffffffffu, pincl, 31);
@@ -211,8 +212,8 @@ int dv_ray_pe(int kind, int channels, const float* params, int batch, const floa
 }
 
 int dv_decode_fwd(int kind, int channels, const float* params, const float* voxels, int nvx, int nvy, int nvz,
-                  const float* seg, const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
-                  void* stream) {
+                  const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                  const float* pe_out, float* out4, void* stream) {
   DecodeArgs a{};
   DV_CHECK(fill_layers(a, kind, channels) == DV_OK && n_seg >= 0, DV_ERR_ARG);
   if (n_seg == 0) return DV_OK;
@@ -225,6 +226,7 @@ int dv_decode_fwd(int kind, int channels, const float* params, const float* voxe
   a.seg = seg;
   a.seg_ray = seg_ray;
   a.S = n_seg;
+  a.S_dev = n_seg_dev;
   a.params = params;
   a.pe_out = const_cast<float*>(pe_out);
   a.out4 = reinterpret_cast<float4*>(out4);
@@ -255,7 +257,7 @@ int dv_composite_fwd(int batch, const int64_t* offsets, const float* out4, int w
 }
 
 int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4, const float* rgb, const float* grad_rgb,
-                     float reg_coef, float* d4, void* stream) {
+                     float reg_coef, const float* reg_scale, float* d4, void* stream) {
   DV_CHECK(batch >= 0, DV_ERR_ARG);
   if (batch == 0) return DV_OK;
   DV_CHECK(offsets && out4 && rgb && grad_rgb && d4, DV_ERR_ARG);
@@ -266,6 +268,7 @@ int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4, const
   a.rgb = const_cast<float*>(rgb);
   a.g_rgb = grad_rgb;
   a.reg_coef = reg_coef;
+  a.reg_scale = reg_scale;
   composite_bwd_kernel<<<ceil_div((long long)batch * 32, 256), 256, 0, (cudaStream_t)stream>>>(
       a, reinterpret_cast<float4*>(d4));
   DV_TRY_LAUNCH();
@@ -273,8 +276,9 @@ int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4, const
 }
 
 int dv_decode_bwd(int kind, int channels, const float* params, const float* voxels, int nvx, int nvy, int nvz,
-                  const float* seg, const int* seg_ray, long long n_seg, const float* pe_feat, const float* pe_out,
-                  const float* d4, float* grad_voxels, float* grad_params, void* stream) {
+                  const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                  const float* pe_feat, const float* pe_out, const float* d4, float* grad_voxels, float* grad_params,
+                  void* stream) {
   DecodeArgs a{};
   DV_CHECK(fill_layers(a, kind, channels) == DV_OK && n_seg >= 0, DV_ERR_ARG);
   if (n_seg == 0) return DV_OK;
@@ -288,6 +292,7 @@ int dv_decode_bwd(int kind, int channels, const float* params, const float* voxe
   a.seg = seg;
   a.seg_ray = seg_ray;
   a.S = n_seg;
+  a.S_dev = n_seg_dev;
   a.params = params;
   a.pe_feat = const_cast<float*>(pe_feat);
   a.pe_out = const_cast<float*>(pe_out);

@@ -29,7 +29,8 @@ struct DecodeArgs {
   int nvx, nvy, nvz;
   const float* seg;        // [S][6]
   const int* seg_ray;      // [S]
-  long long S;
+  long long S;             // segment count, or capacity when S_dev is set
+  const int64_t* S_dev;    // optional device-held count (clamped to S)
   const int64_t* offsets;  // [B+1]
   int B;
   const float* params;     // packed plain layout
@@ -48,7 +49,8 @@ struct DecodeArgs {
   float* t_final;          // [B] or null
   float* reg_sum;          // [B] or null: sum of log(1 + sigma^2 / 0.5)
   const float* g_rgb;      // [B][3] dL/drgb
-  float reg_coef;          // l_s / (B * M)
+  float reg_coef;          // l_s / (B * M), or l_s / B with reg_scale = 1 / M
+  const float* reg_scale;  // optional device factor on reg_coef
 };
 
 // Layer indices: 0 .. D1-1 hidden layers of mlp1 (first: C -> W), D1: mlp1
@@ -56,7 +58,7 @@ struct DecodeArgs {
 // (W+27 -> W), D1+2: mlp2 output (W -> 3).
 
 template <int C, int TILE>
-__device__ __forceinline__ void gather_tile(const DecodeArgs& a, long long s0, float* X0) {
+__device__ __forceinline__ void gather_tile(const DecodeArgs& a, long long S, long long s0, float* X0) {
   constexpr int TPS = C / 4;
   constexpr int SPP = TILE / TPS;
   const int t = threadIdx.x;
@@ -66,7 +68,7 @@ __device__ __forceinline__ void gather_tile(const DecodeArgs& a, long long s0, f
     const int q = t % TPS;
     const long long s = s0 + ls;
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (s < a.S) {
+    if (s < S) {
       const float* sg = a.seg + s * 6;
       const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -77,7 +79,7 @@ __device__ __forceinline__ void gather_tile(const DecodeArgs& a, long long s0, f
 }
 
 template <int C, int TILE>
-__device__ __forceinline__ void scatter_tile(const DecodeArgs& a, long long s0, const float* X0) {
+__device__ __forceinline__ void scatter_tile(const DecodeArgs& a, long long S, long long s0, const float* X0) {
   constexpr int TPS = C / 4;
   constexpr int SPP = TILE / TPS;
   const int t = threadIdx.x;
@@ -86,7 +88,7 @@ __device__ __forceinline__ void scatter_tile(const DecodeArgs& a, long long s0, 
     const int ls = p * SPP + t / TPS;
     const int q = t % TPS;
     const long long s = s0 + ls;
-    if (s < a.S) {
+    if (s < S) {
       const float* sg = a.seg + s * 6;
       const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -185,13 +187,14 @@ __global__ void __launch_bounds__(TILE) decode_fwd_plain(const DecodeArgs a) {
   const int t = threadIdx.x;
   load_weights(a, sw);
   __syncthreads();
-  const long long tiles = (a.S + TILE - 1) / TILE;
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + TILE - 1) / TILE;
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const long long s0 = tile * TILE;
-    gather_tile<C, TILE>(a, s0, X0);
+    gather_tile<C, TILE>(a, S, s0, X0);
     __syncthreads();
     const long long s = s0 + t;
-    if (s < a.S) {
+    if (s < S) {
       a.out4[s] = mlp_forward_rows<C, W, D1, false>(a, sw, X0 + t * (C + 4), __ldg(a.seg_ray + s),
                                                    H0 + t * (W + 4), H1 + t * (W + 4), nullptr, nullptr, nullptr,
                                                    true);
@@ -270,12 +273,13 @@ __global__ void __launch_bounds__(TILE) decode_bwd_plain(const DecodeArgs a) {
   float* A4row = A4 + t * SA;
   float* DLrow = DL + t * SA;
   float* X0row = X0 + t * SX;
-  const long long tiles = (a.S + TILE - 1) / TILE;
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + TILE - 1) / TILE;
   for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const long long s0 = tile * TILE;
     const long long s = s0 + t;
-    const bool valid = s < a.S;
-    gather_tile<C, TILE>(a, s0, X0);
+    const bool valid = s < S;
+    gather_tile<C, TILE>(a, S, s0, X0);
     __syncthreads();
     const int ray = valid ? __ldg(a.seg_ray + s) : 0;
     const float4 c = mlp_forward_rows<C, W, D1, true>(a, sw, X0row, ray, nullptr, nullptr, Arow, A3row, A4row, valid);
@@ -322,7 +326,7 @@ __global__ void __launch_bounds__(TILE) decode_bwd_plain(const DecodeArgs a) {
       for (int k = 0; k < C; k += 4) *reinterpret_cast<float4*>(X0row + k) = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
-    scatter_tile<C, TILE>(a, s0, X0);
+    scatter_tile<C, TILE>(a, S, s0, X0);
     __syncthreads();
   }
   for (int i = threadIdx.x; i < a.n_params; i += TILE)

@@ -39,7 +39,8 @@ struct TcArgs {
   int nvx, nvy, nvz;
   const float* seg;
   const int* seg_ray;
-  long long S;
+  long long S;           // segment count, or capacity when S_dev is set
+  const int64_t* S_dev;  // optional device-held count (clamped to S)
   const float* pe_out;  // [B][W]: bias + PE part of mlp2's first layer (FP32)
   float4* out4;
   const uint8_t* wblob;
@@ -51,7 +52,7 @@ struct TcArgs {
 };
 
 template <int C, int BF16>
-__device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long s0, uint8_t* sA) {
+__device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, long long s0, uint8_t* sA) {
   constexpr int TPS = C / 4;
   constexpr int SPP = 128 / TPS;
   const int t = threadIdx.x;
@@ -61,7 +62,7 @@ __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long s0, ui
     const int q = t % TPS;
     const long long s = s0 + ls;
     float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (s < a.S) {
+    if (s < S) {
       const float* sg = a.seg + s * 6;
       const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -90,7 +91,7 @@ __device__ __forceinline__ void unpack8(const uint4 w, float* f) {
 // Gather from the 16-bit copy of the grid: C/8 threads per segment, each
 // reading 16 bytes (8 channels) of every corner row; the integral is FP32.
 template <int C, int BF16>
-__device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long s0, uint8_t* sA) {
+__device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long S, long long s0, uint8_t* sA) {
   constexpr int TPS = C / 8;
   constexpr int SPP = 128 / TPS;
   const int t = threadIdx.x;
@@ -100,7 +101,7 @@ __device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long s0, ui
     const int q = t % TPS;
     const long long s = s0 + ls;
     float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (s < a.S) {
+    if (s < S) {
       const float* sg = a.seg + s * 6;
       const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4),
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -193,15 +194,16 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
   const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
   uint32_t phase = 0;
   bool ok = true;
-  const long long tiles = (a.S + 127) / 128;
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + 127) / 128;
   for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
     const long long s0 = tile * 128;
     const long long s = s0 + t;
-    const bool valid = s < a.S;
+    const bool valid = s < S;
     if (a.grid16)
-      gather_tile_16<C, BF16>(a, s0, sA);
+      gather_tile_16<C, BF16>(a, S, s0, sA);
     else
-      gather_tile_lp<C, BF16>(a, s0, sA);
+      gather_tile_lp<C, BF16>(a, S, s0, sA);
     sync_for_mma();
     float v[32];
     // mlp1 hidden layers: D = relu(A W^T + b)
@@ -284,23 +286,9 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
   if (warp == 0) tc::tmem_dealloc(tmem, NCOLS);
 }
 
-// CTAs of 128 threads that fit on one SM, from the kernel's registers and
-// shared memory, and never more than TMEM (512 columns) can hold.  (The
-// occupancy API under-reports kernels that allocate TMEM.)
-static int resident_ctas(const void* kernel, size_t dyn_smem, int ncols) {
-  cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
-  int dev = 0, regs_sm = 65536, smem_sm = 228 * 1024, thr_sm = 2048;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
-  const int regs = std::max(fa.numRegs, 1) * 128;
-  const size_t smem = dyn_smem + fa.sharedSizeBytes + 1024;  // + per-CTA reservation
-  int n = std::min({thr_sm / 128, regs_sm / regs, (int)(smem_sm / smem), 512 / ncols});
-  return std::max(n, 1);
-}
-
+// The persistent grid holds as many CTAs per SM as registers, shared memory
+// and TMEM (512 columns) allow together (the occupancy API under-reports
+// kernels that allocate TMEM).
 template <int C, int W, int D1, int BF16>
 int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   constexpr int NCOLS = W == 32 ? 64 : 128;
@@ -311,11 +299,17 @@ int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int per_sm = resident_ctas(reinterpret_cast<const void*>(k), smem, NCOLS);
-  if (per_sm < 1) return DV_ERR_UNSUPPORTED;
+  const tc::Residency res = tc::tmem_residency(reinterpret_cast<const void*>(k), smem, NCOLS, 128);
+  if (res.dyn_smem != smem) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res.dyn_smem) != cudaSuccess)
+      return DV_ERR_CUDA;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
+        cudaSuccess)
+      return DV_ERR_CUDA;
+  }
   const long long tiles = (a.S + 127) / 128;
-  const long long grid = std::min<long long>(tiles, (long long)sms * per_sm);
-  k<<<(unsigned)grid, 128, smem, st>>>(a);
+  const long long grid = std::min<long long>(tiles, (long long)sms * res.per_sm);
+  k<<<(unsigned)grid, 128, res.dyn_smem, st>>>(a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -328,8 +322,8 @@ extern "C" {
 
 int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
                      const int* layers, int n_layers, const float* voxels, const void* voxels16, int nvx, int nvy,
-                     int nvz, const float* seg, const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
-                     int* err, void* stream) {
+                     int nvz, const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                     const float* pe_out, float* out4, int* err, void* stream) {
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
   const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
   DV_CHECK(d1 > 0 && n_layers == d1 + 3 && n_layers <= TC_MAX_LAYERS, DV_ERR_ARG);
@@ -348,6 +342,7 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
   a.seg = seg;
   a.seg_ray = seg_ray;
   a.S = n_seg;
+  a.S_dev = n_seg_dev;
   a.pe_out = pe_out;
   a.out4 = reinterpret_cast<float4*>(out4);
   a.wblob = reinterpret_cast<const uint8_t*>(wblob);

@@ -46,7 +46,8 @@ struct Args {
   int nvx, nvy, nvz;
   const float* seg;
   const int* seg_ray;
-  long long S;
+  long long S;           // segment count, or capacity when S_dev is set
+  const int64_t* S_dev;  // optional device-held count (clamped to S)
   const float* pe_feat;  // [B][28]
   const float* pe_out;   // [B][W]
   const float4* d4;      // [S] (dL/dsigma, dL/drgb)
@@ -199,11 +200,12 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
   float v[48];
 
-  const long long tiles = (a.S + 127) / 128;
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + 127) / 128;
   for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
     const long long s0 = tile * 128;
     const long long s = s0 + t;
-    const bool valid = s < a.S;
+    const bool valid = s < S;
     const int ray = valid ? __ldg(a.seg_ray + s) : 0;
     // ---- gather: feature rows ----
     {
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
         const int ls = pp * SPP + t / TPS, q = t % TPS;
         const long long ss = s0 + ls;
         float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ss < a.S) {
+        if (ss < S) {
           const float* sg = a.seg + ss * 6;
           const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3),
                                                __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
       for (int pp = 0; pp < TPS; ++pp) {
         const int ls = pp * SPP + t / TPS, q = t % TPS;
         const long long ss = s0 + ls;
-        if (ss < a.S) {
+        if (ss < S) {
           const float* sg = a.seg + ss * 6;
           const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3),
                                                __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
@@ -464,18 +466,6 @@ inline size_t smem_bytes(const Args& a) {
 
 }  // namespace bw
 
-static int resident_bwd(const void* kernel, size_t dyn_smem) {
-  cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
-  int dev = 0, regs_sm = 65536, smem_sm = 228 * 1024;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-  const int n = std::min({16, regs_sm / (std::max(fa.numRegs, 1) * 128),
-                          (int)(smem_sm / (dyn_smem + fa.sharedSizeBytes + 1024)), 512 / bw::TMEM_COLS});
-  return std::max(n, 1);
-}
-
 }  // namespace dv
 
 using namespace dv;
@@ -485,8 +475,8 @@ extern "C" {
 int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_bytes, const float* bias, int nbias,
                      const int* f_layers, const void* wb, int wb_bytes, const int* b_layers, int n_layers,
                      const float* voxels, int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
-                     long long n_seg, const float* pe_feat, const float* pe_out, const float* d4, float* grad_voxels,
-                     float* grad_params, int* err, void* stream) {
+                     long long n_seg, const int64_t* n_seg_dev, const float* pe_feat, const float* pe_out,
+                     const float* d4, float* grad_voxels, float* grad_params, int* err, void* stream) {
   using namespace dv::bw;
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
   DV_CHECK(kind == 32 && channels == 32 && n_layers == NL && bf16 == 1, DV_ERR_UNSUPPORTED);
@@ -506,6 +496,7 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
   a.seg = seg;
   a.seg_ray = seg_ray;
   a.S = n_seg;
+  a.S_dev = n_seg_dev;
   a.pe_feat = pe_feat;
   a.pe_out = pe_out;
   a.d4 = reinterpret_cast<const float4*>(d4);
@@ -552,10 +543,17 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int per_sm = resident_bwd(reinterpret_cast<const void*>(k), smem);
+  const tc::Residency res = tc::tmem_residency(reinterpret_cast<const void*>(k), smem, bw::TMEM_COLS, 128);
+  if (res.dyn_smem != smem) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)res.dyn_smem) != cudaSuccess)
+      return DV_ERR_CUDA;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared) !=
+        cudaSuccess)
+      return DV_ERR_CUDA;
+  }
   const long long tiles = (n_seg + 127) / 128;
-  const long long grid = std::min<long long>(tiles, (long long)sms * per_sm);
-  k<<<(unsigned)grid, 128, smem, (cudaStream_t)stream>>>(a);
+  const long long grid = std::min<long long>(tiles, (long long)sms * res.per_sm);
+  k<<<(unsigned)grid, 128, res.dyn_smem, (cudaStream_t)stream>>>(a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

@@ -140,5 +140,53 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
   return r;
 }
 
+// Residency of a persistent kernel whose CTAs each allocate `ncols` TMEM
+// columns.  Registers and shared memory may admit more CTAs per SM than the
+// 512 TMEM columns can hold; a CTA scheduled beyond that waits inside
+// tcgen05.alloc until a resident CTA has finished its whole share of the
+// tiles, which stretches that SM to about twice the others.  The dynamic
+// shared memory is therefore padded until shared memory alone admits no more
+// CTAs than the TMEM does, and the kernel asks for the largest shared-memory
+// carveout so that the padded count is what the SM really holds.
+struct Residency {
+  int per_sm;       // CTAs per SM the launch may count on (>= 1)
+  size_t dyn_smem;  // dynamic shared memory to launch with (>= the request)
+};
+
+inline Residency tmem_residency(const void* kernel, size_t dyn_smem, int ncols, int threads) {
+  Residency r{1, dyn_smem};
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return r;
+  int dev = 0, regs_sm = 65536, smem_sm = 228 * 1024, thr_sm = 2048, reserved = 1024;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  const size_t fixed = fa.sharedSizeBytes + (size_t)reserved;
+  const int by_threads = thr_sm / threads;
+  const int by_regs = regs_sm / (fa.numRegs > 0 ? fa.numRegs * threads : threads);
+  const int by_smem = (int)(smem_sm / (dyn_smem + fixed));
+  const int by_tmem = 512 / ncols;
+  int n = by_threads < by_regs ? by_threads : by_regs;
+  n = n < by_tmem ? n : by_tmem;
+  if (n >= by_smem) {
+    r.per_sm = by_smem > 0 ? by_smem : 1;
+    return r;
+  }
+  // Pad: (n + 1) CTAs must no longer fit, n still must.
+  size_t per_cta = (size_t)smem_sm / (size_t)(n + 1) + 1;
+  size_t dyn = per_cta > fixed ? per_cta - fixed : 0;
+  dyn = (dyn + 127) / 128 * 128;
+  if (dyn < dyn_smem) dyn = dyn_smem;
+  if ((size_t)n * (dyn + fixed) > (size_t)smem_sm) {
+    r.per_sm = by_smem < by_tmem ? by_smem : by_tmem;  // cannot pad exactly; stay within both limits
+    return r;
+  }
+  r.per_sm = n;
+  r.dyn_smem = dyn;
+  return r;
+}
+
 }  // namespace tc
 }  // namespace dv

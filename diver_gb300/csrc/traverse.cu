@@ -28,6 +28,7 @@ struct WalkArgs {
   float mask_scale;
   int m;            // occupancy cells per side
   long long cells;  // m^3
+  bool fast;        // grid small enough for the reciprocal-based division (< 2^22 voxels per side)
   const float* o;
   const float* v;
   const uint8_t* mask;
@@ -69,6 +70,39 @@ __device__ __forceinline__ float3 signs(float3 d) {
 
 // Dense walk: entry point, then every plane crossing while the point stays
 // in [0,n]^3.  Reference ray_voxel_intersect.cu:39-150.
+template <int MODE, bool FAST>
+__device__ __forceinline__ int dense_walk(const WalkArgs& a, int b, float3 p, const float3 d, float t, float* row,
+                                          float* trow, int64_t base, int64_t cap) {
+  const float3 s = signs(d);
+  const float3 r = FAST ? recip3(d) : d;
+  int count = 1;
+  float3 q;
+  float dt;
+  while (true) {
+    grid_step<FAST>(p, d, r, s, q, dt);
+    const float tq = __fadd_rn(t, dt);
+    if (outside_closed(q, a.n)) break;
+    if (MODE == WALK_PADDED && count < a.max_n) {
+      row[3 * count + 0] = q.x;
+      row[3 * count + 1] = q.y;
+      row[3 * count + 2] = q.z;
+      trow[count] = __fmul_rn(tq, a.voxel_size);
+    }
+    if (MODE == WALK_SEGMENTS && count - 1 < cap) {
+      float2* sg = reinterpret_cast<float2*>(a.seg + (base + count - 1) * 6);
+      sg[0] = make_float2(p.x, p.y);
+      sg[1] = make_float2(p.z, q.x);
+      sg[2] = make_float2(q.y, q.z);
+      if (a.seg_t) a.seg_t[base + count - 1] = __fmul_rn(t, a.voxel_size);
+      if (a.seg_ray) a.seg_ray[base + count - 1] = b;
+    }
+    ++count;
+    p = q;
+    t = tq;
+  }
+  return count;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) dense_walk_kernel(const WalkArgs a) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -97,43 +131,113 @@ __global__ void __launch_bounds__(256) dense_walk_kernel(const WalkArgs a) {
     }
     if (hit) {
       if (MODE == WALK_PADDED && a.max_n > 0) trow[0] = __fmul_rn(t, a.voxel_size);
-      count = 1;
-      const float3 s = signs(d);
-      float3 q;
-      float dt;
-      while (true) {
-        grid_step(p, d, s, q, dt);
-        const float tq = __fadd_rn(t, dt);
-        if (outside_closed(q, a.n)) break;
-        if (MODE == WALK_PADDED && count < a.max_n) {
-          row[3 * count + 0] = q.x;
-          row[3 * count + 1] = q.y;
-          row[3 * count + 2] = q.z;
-          trow[count] = __fmul_rn(tq, a.voxel_size);
-        }
-        if (MODE == WALK_SEGMENTS && count - 1 < cap) {
-          float* sg = a.seg + (base + count - 1) * 6;
-          sg[0] = p.x;
-          sg[1] = p.y;
-          sg[2] = p.z;
-          sg[3] = q.x;
-          sg[4] = q.y;
-          sg[5] = q.z;
-          if (a.seg_t) a.seg_t[base + count - 1] = __fmul_rn(t, a.voxel_size);
-          if (a.seg_ray) a.seg_ray[base + count - 1] = b;
-        }
-        ++count;
-        p = q;
-        t = tq;
-      }
+      count = (a.fast && recip_ok(d)) ? dense_walk<MODE, true>(a, b, p, d, t, row, trow, base, cap)
+                          : dense_walk<MODE, false>(a, b, p, d, t, row, trow, base, cap);
     }
     if (MODE != WALK_SEGMENTS) a.num[b] = count;
   }
   if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
 }
 
+// Segment record writer for the compacted (CSR) output.  A segment at an even
+// global index is held back in registers; its successor then goes out with it
+// as one 48-byte pair (three aligned 16-byte stores of the six coordinates,
+// 8-byte stores of the two t and ray values).  A segment that has no
+// successor slot, or that sits at an odd index with nothing held, is written
+// alone (8-byte stores).  Needs seg 16-byte and seg_t / seg_ray 8-byte aligned
+// buffers, which the entry points check.
+struct SegWriter {
+  float h[7];  // held segment: entry xyz, exit xyz, t
+  int64_t hi;  // its global index, -1 when nothing is held
+  __device__ __forceinline__ SegWriter() : hi(-1) {}
+
+  __device__ __forceinline__ void single(const WalkArgs& a, int b, int64_t g, const float* v, float t) {
+    float2* sg = reinterpret_cast<float2*>(a.seg + g * 6);
+    sg[0] = make_float2(v[0], v[1]);
+    sg[1] = make_float2(v[2], v[3]);
+    sg[2] = make_float2(v[4], v[5]);
+    if (a.seg_t) a.seg_t[g] = t;
+    if (a.seg_ray) a.seg_ray[g] = b;
+  }
+
+  __device__ __forceinline__ void put(const WalkArgs& a, int b, int64_t g, bool has_next, const float3 p,
+                                      const float3 q, float t) {
+    if (hi >= 0) {  // g == hi + 1, hi even
+      float4* s4 = reinterpret_cast<float4*>(a.seg + hi * 6);
+      s4[0] = make_float4(h[0], h[1], h[2], h[3]);
+      s4[1] = make_float4(h[4], h[5], p.x, p.y);
+      s4[2] = make_float4(p.z, q.x, q.y, q.z);
+      if (a.seg_t) *reinterpret_cast<float2*>(a.seg_t + hi) = make_float2(h[6], t);
+      if (a.seg_ray) *reinterpret_cast<int2*>(a.seg_ray + hi) = make_int2(b, b);
+      hi = -1;
+    } else if (((g & 1) == 0) && has_next) {
+      h[0] = p.x;
+      h[1] = p.y;
+      h[2] = p.z;
+      h[3] = q.x;
+      h[4] = q.y;
+      h[5] = q.z;
+      h[6] = t;
+      hi = g;
+    } else {
+      const float v[6] = {p.x, p.y, p.z, q.x, q.y, q.z};
+      single(a, b, g, v, t);
+    }
+  }
+
+  __device__ __forceinline__ void flush(const WalkArgs& a, int b) {
+    if (hi >= 0) single(a, b, hi, h, h[6]);
+    hi = -1;
+  }
+};
+
 // Masked walk: (entry, exit) of every voxel whose occupancy byte is set.
 // Reference ray_voxel_intersect.cu:203-318.
+template <int MODE, bool FAST>
+__device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, const float3 d, float t) {
+  const float3 s = signs(d);
+  const float3 r = FAST ? recip3(d) : d;
+  float* row = nullptr;
+  float* trow = nullptr;
+  int64_t base = 0, cap = 0;
+  if (MODE == WALK_PADDED) {
+    row = a.inter + (long long)b * a.max_n * 6;
+    trow = a.tns + (long long)b * a.max_n;
+  }
+  if (MODE == WALK_SEGMENTS) {
+    base = a.offsets[b];
+    cap = a.offsets[b + 1] - base;
+  }
+  SegWriter w;
+  int count = 0;
+  float3 q;
+  float dt;
+  while (true) {
+    grid_step<FAST>(p, d, r, s, q, dt);
+    t = __fadd_rn(t, dt);
+    if (outside_closed3(q, a.n3)) break;
+    const long long idx = cell_index3(p, q, a.mask_scale, a.mx, a.my);
+    if (occupied(a.mask, idx, a.cells)) {
+      if (MODE == WALK_PADDED && count < a.max_n) {
+        float* rr = row + 6 * count;
+        rr[0] = p.x;
+        rr[1] = p.y;
+        rr[2] = p.z;
+        rr[3] = q.x;
+        rr[4] = q.y;
+        rr[5] = q.z;
+        trow[count] = __fmul_rn(t, a.voxel_size);
+      }
+      if (MODE == WALK_SEGMENTS && count < cap)
+        w.put(a, b, base + count, count + 1 < cap, p, q, __fmul_rn(t, a.voxel_size));
+      ++count;
+    }
+    p = q;
+  }
+  if (MODE == WALK_SEGMENTS) w.flush(a, b);
+  return count;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -143,53 +247,8 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
     const float3 d = load3(a.v, b);
     float3 p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
     float t;
-    if (box_entry3(p, d, a.n3, t)) {
-      const float3 s = signs(d);
-      float* row = nullptr;
-      float* trow = nullptr;
-      int64_t base = 0, cap = 0;
-      if (MODE == WALK_PADDED) {
-        row = a.inter + (long long)b * a.max_n * 6;
-        trow = a.tns + (long long)b * a.max_n;
-      }
-      if (MODE == WALK_SEGMENTS) {
-        base = a.offsets[b];
-        cap = a.offsets[b + 1] - base;
-      }
-      float3 q;
-      float dt;
-      while (true) {
-        grid_step(p, d, s, q, dt);
-        t = __fadd_rn(t, dt);
-        if (outside_closed3(q, a.n3)) break;
-        const long long idx = cell_index3(p, q, a.mask_scale, a.mx, a.my);
-        if (occupied(a.mask, idx, a.cells)) {
-          if (MODE == WALK_PADDED && count < a.max_n) {
-            float* r = row + 6 * count;
-            r[0] = p.x;
-            r[1] = p.y;
-            r[2] = p.z;
-            r[3] = q.x;
-            r[4] = q.y;
-            r[5] = q.z;
-            trow[count] = __fmul_rn(t, a.voxel_size);
-          }
-          if (MODE == WALK_SEGMENTS && count < cap) {
-            float* sg = a.seg + (base + count) * 6;
-            sg[0] = p.x;
-            sg[1] = p.y;
-            sg[2] = p.z;
-            sg[3] = q.x;
-            sg[4] = q.y;
-            sg[5] = q.z;
-            if (a.seg_t) a.seg_t[base + count] = __fmul_rn(t, a.voxel_size);
-            if (a.seg_ray) a.seg_ray[base + count] = b;
-          }
-          ++count;
-        }
-        p = q;
-      }
-    }
+    if (box_entry3(p, d, a.n3, t))
+      count = (a.fast && recip_ok(d)) ? masked_walk<MODE, true>(a, b, p, d, t) : masked_walk<MODE, false>(a, b, p, d, t);
     if (MODE != WALK_SEGMENTS) a.num[b] = count;
   }
   if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
@@ -197,6 +256,39 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
 
 // Octree first hit.  Reference ray_march.cu:33-148, generalised from the
 // N in {128, 256} templates to any N that is a multiple of 64.
+template <bool FAST>
+__device__ __forceinline__ void octree_descend(float* slot, uint8_t* finish, int b, float3 p, const float3 d,
+                                               const uint8_t* __restrict__ oct, int N, long long oct_cells) {
+  const float3 s = signs(d);
+  const float3 r = FAST ? recip3(d) : d;
+  int m = N / 64;
+  long long off = 0;
+  float3 last = p;
+  while (m < N) {
+    last = p;
+    float3 q;
+    float dt;
+    grid_step<FAST>(last, d, r, s, q, dt);
+    if (outside_closed(q, (float)m)) {
+      slot[0] = -1.f;
+      finish[b] = 1;
+      return;
+    }
+    const long long idx = off + cell_index1(last, q, m);
+    if (occupied(oct, idx, oct_cells)) {
+      off += (long long)m * m * m;
+      last = make_float3(__fmul_rn(last.x, 4.f), __fmul_rn(last.y, 4.f), __fmul_rn(last.z, 4.f));
+      p = last;
+      m *= 4;
+    } else {
+      p = q;
+    }
+  }
+  slot[0] = last.x;
+  slot[1] = last.y;
+  slot[2] = last.z;
+}
+
 __global__ void __launch_bounds__(256) aabb_kernel(int batch, float* __restrict__ coords,
                                                    const float* __restrict__ v,
                                                    const float* __restrict__ center,
@@ -218,39 +310,43 @@ __global__ void __launch_bounds__(256) aabb_kernel(int batch, float* __restrict_
     return;
   }
   p = make_float3(__fmul_rn(p.x, 0.015625f), __fmul_rn(p.y, 0.015625f), __fmul_rn(p.z, 0.015625f));
-  const float3 s = signs(d);
-  int m = N / 64;
-  long long off = 0;
-  float3 last = p;
-  while (m < N) {
-    last = p;
-    float3 q;
-    float dt;
-    grid_step(last, d, s, q, dt);
-    if (outside_closed(q, (float)m)) {
-      slot[0] = -1.f;
-      finish[b] = 1;
-      return;
-    }
-    const long long idx = off + cell_index1(last, q, m);
-    if (occupied(oct, idx, oct_cells)) {
-      off += (long long)m * m * m;
-      last = make_float3(__fmul_rn(last.x, 4.f), __fmul_rn(last.y, 4.f), __fmul_rn(last.z, 4.f));
-      p = last;
-      m *= 4;
-    } else {
-      p = q;
-    }
-  }
-  slot[0] = last.x;
-  slot[1] = last.y;
-  slot[2] = last.z;
+  if (N < (1 << 22) && recip_ok(d))
+    octree_descend<true>(slot, finish, b, p, d, oct, N, oct_cells);
+  else
+    octree_descend<false>(slot, finish, b, p, d, oct, N, oct_cells);
 }
 
 // Next 8 occupied voxels.  Reference ray_march.cu:159-229.  The reference
 // leaves its grid-stride loop when an unfinished ray has no resume point
 // (x < 0), a state that aabb_intersect + mlp_eval never produce; here such a
 // ray is skipped on its own so the result does not depend on the launch shape.
+template <bool FAST>
+__device__ __forceinline__ void march8(float* __restrict__ coords, long long stride, int b, float3 last,
+                                       const float3 d, const uint8_t* __restrict__ mask, int N) {
+  const float3 s = signs(d);
+  const float3 r = FAST ? recip3(d) : d;
+  const float n = (float)N;
+  const long long cells = (long long)N * N * N;
+  int hits = 0;
+  while (hits < 8) {
+    float3 q;
+    float dt;
+    grid_step<FAST>(last, d, r, s, q, dt);
+    if (outside_open(q, n)) {
+      coords[hits * stride + (long long)b * 6] = -1.f;
+      break;
+    }
+    if (occupied(mask, cell_index1(last, q, N), cells)) {
+      float2* rr = reinterpret_cast<float2*>(coords + hits * stride + (long long)b * 6);
+      rr[0] = make_float2(last.x, last.y);
+      rr[1] = make_float2(last.z, q.x);
+      rr[2] = make_float2(q.y, q.z);
+      ++hits;
+    }
+    last = q;
+  }
+}
+
 __global__ void __launch_bounds__(256) march_kernel(int batch, float* __restrict__ coords,
                                                     const float* __restrict__ v,
                                                     const uint8_t* __restrict__ mask,
@@ -263,30 +359,11 @@ __global__ void __launch_bounds__(256) march_kernel(int batch, float* __restrict
   coords[(long long)b * 6] = -1.f;
   if (last.x < 0.f) return;
   const float3 d = load3(v, b);
-  const float3 s = signs(d);
-  const float n = (float)N;
-  const long long cells = (long long)N * N * N;
-  int hits = 0;
-  while (hits < 8) {
-    float3 q;
-    float dt;
-    grid_step(last, d, s, q, dt);
-    if (outside_open(q, n)) {
-      coords[hits * stride + (long long)b * 6] = -1.f;
-      break;
-    }
-    if (occupied(mask, cell_index1(last, q, N), cells)) {
-      float* r = coords + hits * stride + (long long)b * 6;
-      r[0] = last.x;
-      r[1] = last.y;
-      r[2] = last.z;
-      r[3] = q.x;
-      r[4] = q.y;
-      r[5] = q.z;
-      ++hits;
-    }
-    last = q;
-  }
+  const float lim = (float)N;  // a resume point from outside the grid takes the __fdiv_rn form
+  if (N < (1 << 22) && recip_ok(d) && fabsf(last.x) <= lim && fabsf(last.y) <= lim && fabsf(last.z) <= lim)
+    march8<true>(coords, stride, b, last, d, mask, N);
+  else
+    march8<false>(coords, stride, b, last, d, mask, N);
 }
 
 __global__ void pair_counts_kernel(int batch, const int* __restrict__ num, int* __restrict__ out) {
@@ -383,6 +460,14 @@ static int cells_per_side(float n, float scale) {
   return (int)prod;
 }
 
+static bool aligned_to(const void* p, uintptr_t n) { return ((uintptr_t)p % n) == 0; }
+
+// The segment writers store seg with 16-byte (masked) or 8-byte (dense)
+// vector stores and seg_t / seg_ray in 8-byte pairs.
+static bool segment_buffers_aligned(const float* seg, const float* seg_t, const int* seg_ray, uintptr_t seg_align) {
+  return aligned_to(seg, seg_align) && aligned_to(seg_t, 8) && aligned_to(seg_ray, 8);
+}
+
 static WalkArgs walk_args(int batch, float xyzmin, float n, float vs, float mask_scale,
                           const float* o, const float* v, const uint8_t* mask) {
   WalkArgs a{};
@@ -396,6 +481,7 @@ static WalkArgs walk_args(int batch, float xyzmin, float n, float vs, float mask
   a.m = cells_per_side(n, mask_scale);
   a.mx = a.my = a.m;
   a.cells = (long long)a.m * a.m * a.m;
+  a.fast = n < 4194304.f;
   a.o = o;
   a.v = v;
   a.mask = mask;
@@ -476,6 +562,7 @@ int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxe
   DV_CHECK(batch_size >= 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
+  DV_CHECK(segment_buffers_aligned(seg, seg_t, seg_ray, 16), DV_ERR_ARG);
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
   a.offsets = offsets;
   a.seg = seg;
@@ -492,6 +579,7 @@ int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, float voxel
   DV_CHECK(batch_size >= 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && offsets && seg, DV_ERR_ARG);
+  DV_CHECK(segment_buffers_aligned(seg, seg_t, seg_ray, 8), DV_ERR_ARG);
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, 1.f, o, v, nullptr);
   a.offsets = offsets;
   a.seg = seg;
@@ -524,6 +612,7 @@ static WalkArgs walk_args_grid(int batch, const float* xyzmin, const int* dims, 
   a.mx = dims[0];
   a.my = dims[1];
   a.cells = (long long)dims[0] * dims[1] * dims[2];
+  a.fast = dims[0] < (1 << 22) && dims[1] < (1 << 22) && dims[2] < (1 << 22);
   a.o = o;
   a.v = v;
   a.mask = mask;
@@ -549,6 +638,7 @@ int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims
   DV_CHECK(batch_size >= 0 && xyzmin && dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
+  DV_CHECK(segment_buffers_aligned(seg, seg_t, seg_ray, 16), DV_ERR_ARG);
   WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
   a.offsets = offsets;
   a.seg = seg;
@@ -602,6 +692,7 @@ int dv_ray_march(int batch_size, float* coords, const float* v, const uint8_t* m
   DV_CHECK(batch_size >= 0 && voxel_num > 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(coords && v && mask && finish, DV_ERR_ARG);
+  DV_CHECK(aligned_to(coords, 8), DV_ERR_ARG);
   march_kernel<<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(batch_size, coords, v, mask,
                                                                            finish, voxel_num);
   DV_TRY_LAUNCH();

@@ -224,22 +224,31 @@ def tc_matrices(dec: Decoder):
     return mats
 
 
+def _kmajor_images(mats, dt) -> tuple[list[torch.Tensor], list[tuple[int, int, int]]]:
+    """Each [N][K] matrix as a flat K-major core-matrix image of dtype dt, with
+    its (byte offset of a 2-byte element image, K, N)."""
+    images, table, off = [], [], 0
+    for m in mats:
+        N, K = m.shape
+        img = torch.zeros(N * K, dtype=dt)
+        img[_kmajor_index(N, K)] = m.reshape(-1).to(dt)
+        images.append(img)
+        table.append((off, K, N))
+        off += N * K * 2
+    return images, table
+
+
 def pack_tc(dec: Decoder, bf16: bool = True):
     """(blob uint8 [bytes], bias float32, layers int32 [n, 4] = (byte offset, K, N, bias offset))."""
     dt = torch.bfloat16 if bf16 else torch.float16
-    images, biases, table = [], [], []
-    off = 0
-    boff = 0
-    for w, b in tc_matrices(dec):
-        N, K = w.shape
-        img = torch.zeros(N * K, dtype=dt)
-        img[_kmajor_index(N, K)] = w.reshape(-1).to(dt)
-        images.append(img.view(torch.uint8))
-        biases.append(b)
-        table.append([off, K, N, boff])
-        off += N * K * 2
-        boff += N
-    return torch.cat(images), torch.cat(biases).float(), torch.tensor(table, dtype=torch.int32)
+    mats = tc_matrices(dec)
+    images, table = _kmajor_images([w for w, _ in mats], dt)
+    boffs = [0]
+    for _, b in mats[:-1]:
+        boffs.append(boffs[-1] + b.numel())
+    rows = [[off, K, N, bo] for (off, K, N), bo in zip(table, boffs)]
+    return (torch.cat([i.view(torch.uint8) for i in images]), torch.cat([b for _, b in mats]).float(),
+            torch.tensor(rows, dtype=torch.int32))
 
 
 def tc_bwd_matrices(dec: Decoder):
@@ -260,13 +269,27 @@ def tc_bwd_matrices(dec: Decoder):
 def pack_tc_bwd(dec: Decoder, bf16: bool = True):
     """(blob uint8, layers int32 [n, 3] = (byte offset, K, N)) of tc_bwd_matrices."""
     dt = torch.bfloat16 if bf16 else torch.float16
-    images, table = [], []
-    off = 0
-    for m in tc_bwd_matrices(dec):
-        N, K = m.shape
-        img = torch.zeros(N * K, dtype=dt)
-        img[_kmajor_index(N, K)] = m.reshape(-1).to(dt)
-        images.append(img.view(torch.uint8))
-        table.append([off, K, N])
-        off += N * K * 2
-    return torch.cat(images), torch.tensor(table, dtype=torch.int32)
+    images, table = _kmajor_images(tc_bwd_matrices(dec), dt)
+    return torch.cat([i.view(torch.uint8) for i in images]), torch.tensor(table, dtype=torch.int32)
+
+
+def tc_index_maps(kind: str, channels: int) -> dict:
+    """Where every element of the tensor-core images comes from in the packed
+    plain parameter vector: index + 1, or 0 for padding.  The images are pure
+    rearrangements of the parameters, so a gather of the (zero-prefixed)
+    parameter vector rebuilds them on the device, e.g. after an optimizer step,
+    without a host round trip.  Keys: 'fwd' (element indices of pack_tc's blob
+    as 2-byte elements), 'bias', 'table' (pack_tc's layer rows), and for
+    DIVeR32 over 32 channels 'bwd' / 'bwd_table' (pack_tc_bwd)."""
+    n = plain_size(kind, channels)
+    ids = torch.arange(1, n + 1, dtype=torch.float32)  # exact in float32 (n < 2^24)
+    dec = Decoder(kind, channels, unpack_plain_grad(kind, channels, ids))
+    mats = tc_matrices(dec)
+    images, _ = _kmajor_images([w for w, _ in mats], torch.float32)
+    _, _, table = pack_tc(dec, True)
+    out = {"fwd": torch.cat(images).long(), "bias": torch.cat([b for _, b in mats]).long(), "table": table}
+    if kind == "diver32" and channels == 32:
+        bim, btab = _kmajor_images(tc_bwd_matrices(dec), torch.float32)
+        out["bwd"] = torch.cat(bim).long()
+        out["bwd_table"] = torch.tensor(btab, dtype=torch.int32)
+    return out

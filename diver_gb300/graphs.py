@@ -1,0 +1,94 @@
+"""CUDA-graph forms of the training step and of frame rendering.
+
+The eager pipeline reads two numbers back to the host per step (the segment
+count, to size the segment buffers, and the longest ray, for the sparsity
+term's mean over the padded [B, M]) and pays Python and launch overhead for
+about twenty launches.  With fixed-capacity segment buffers
+(`DIVeRField.segments(..., capacity)`) both numbers stay on the device, every
+launch reads its sizes there, and the whole step, traversal through weight
+gradients, is recorded once in a CUDA graph and replayed.
+
+  TrainStepGraph   loss = mse(rgb, target) + l_s * reg and its gradients for
+                   the feature grid and the packed decoder parameters
+                   (train.py:84-85,109-113), for a fixed batch size
+  RenderGraph      rgb of a fixed number of rays (no autograd)
+
+Inputs are copied into the graph's own buffers before each replay; outputs
+are the graph's buffers (overwritten by the next replay; clone to keep them).
+The tensor-core weight images are repacked from the parameters inside the
+graph, so optimizer steps between replays are seen by the next replay.
+"""
+from __future__ import annotations
+
+import torch
+
+from .renderer import DIVeRField
+
+
+def _warm_and_capture(fn, warmup: int):
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(warmup):
+            fn()
+    torch.cuda.current_stream().wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        out = fn()
+    return graph, out
+
+
+class TrainStepGraph:
+    """One captured training step of `field` on batches shaped like the
+    example (o [B,3], d [B,3], target [B,3])."""
+
+    def __init__(self, field: DIVeRField, o: torch.Tensor, d: torch.Tensor, target: torch.Tensor,
+                 form: str = "bf16", l_s: float = 1e-5, warmup: int = 2):
+        self.field, self.form, self.l_s = field, form, float(l_s)
+        self.o, self.d, self.target = o.clone().contiguous(), d.clone().contiguous(), target.clone().contiguous()
+        self.capacity = field.segment_capacity(o.shape[0])
+        field.refresh_always = True
+        try:
+            self.graph, (self.loss, self.grad_voxels, self.grad_params) = _warm_and_capture(self._step, warmup)
+        finally:
+            field.refresh_always = False
+
+    def _step(self):
+        f = self.field
+        rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity)
+        loss = torch.nn.functional.mse_loss(rgb, self.target) + self.l_s * reg
+        gv, gp = torch.autograd.grad(loss, [f.voxels, f.params])
+        return loss.detach(), gv, gp
+
+    def __call__(self, o: torch.Tensor, d: torch.Tensor, target: torch.Tensor):
+        """(loss, grad_voxels, grad_params) of this batch (graph buffers)."""
+        self.o.copy_(o, non_blocking=True)
+        self.d.copy_(d, non_blocking=True)
+        self.target.copy_(target, non_blocking=True)
+        self.graph.replay()
+        return self.loss, self.grad_voxels, self.grad_params
+
+
+class RenderGraph:
+    """Captured forward render of B rays (o, d like the example)."""
+
+    def __init__(self, field: DIVeRField, o: torch.Tensor, d: torch.Tensor, form: str = "bf16", warmup: int = 2):
+        self.field, self.form = field, form
+        self.o, self.d = o.clone().contiguous(), d.clone().contiguous()
+        self.capacity = field.segment_capacity(o.shape[0])
+        field.refresh_always = True
+        try:
+            with torch.no_grad():
+                self.graph, self.rgb = _warm_and_capture(self._render, warmup)
+        finally:
+            field.refresh_always = False
+
+    def _render(self):
+        rgb, _ = self.field(self.o, self.d, form=self.form, capacity=self.capacity)
+        return rgb
+
+    def __call__(self, o: torch.Tensor, d: torch.Tensor) -> torch.Tensor:
+        self.o.copy_(o, non_blocking=True)
+        self.d.copy_(d, non_blocking=True)
+        self.graph.replay()
+        return self.rgb

@@ -121,13 +121,21 @@ class Segments:
 
     offsets [B+1] int64, seg [S, 6] float32 (entry xyz, exit xyz, voxel units),
     t [S] float32 distances, ray [S] int32 ray index, counts [B] int32.
+
+    Built with a fixed `capacity`, the buffers hold that many rows and only the
+    first offsets[B] are segments; the count (offsets[B]) and max_dev (max
+    segments per ray, int32 [1]) then stay on the device and max_count is None.
     """
 
-    __slots__ = ("offsets", "seg", "t", "ray", "counts", "max_count")
+    __slots__ = ("offsets", "seg", "t", "ray", "counts", "max_count", "max_dev")
 
-    def __init__(self, offsets, seg, t, ray, counts, max_count=None):
+    def __init__(self, offsets, seg, t, ray, counts, max_count=None, max_dev=None):
         self.offsets, self.seg, self.t, self.ray, self.counts = offsets, seg, t, ray, counts
-        self.max_count = int(counts.max()) if max_count is None and counts.numel() else (max_count or 0)
+        self.max_dev = max_dev
+        if max_dev is not None:
+            self.max_count = max_count
+        else:
+            self.max_count = int(counts.max()) if max_count is None and counts.numel() else (max_count or 0)
 
     @property
     def coord_in(self) -> torch.Tensor:
@@ -139,7 +147,15 @@ class Segments:
 
     @property
     def total(self) -> int:
+        """Rows of the buffers: the segment count, or the capacity."""
         return self.seg.shape[0]
+
+    @property
+    def count_ptr(self) -> int | None:
+        """Device address of the segment count (offsets[B]) for the decode entry points."""
+        if self.offsets.numel() == 0:
+            return None
+        return self.offsets.data_ptr() + (self.offsets.numel() - 1) * self.offsets.element_size()
 
 
 def _totals(offsets: torch.Tensor, counts: torch.Tensor) -> tuple[int, int]:
@@ -150,30 +166,46 @@ def _totals(offsets: torch.Tensor, counts: torch.Tensor) -> tuple[int, int]:
     return int(S), int(M)
 
 
-def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale) -> Segments:
+def _capacity(capacity: int, B: int, planes: int) -> int:
+    need = B * (planes + 3)
+    if capacity < need:
+        raise ValueError(f"capacity {capacity} is below the {need} segments that {B} rays can produce")
+    return int(capacity)
+
+
+def _buffers(S: int, dev):
+    return (torch.empty(S, 6, dtype=torch.float32, device=dev), torch.empty(S, dtype=torch.float32, device=dev),
+            torch.empty(S, dtype=torch.int32, device=dev))
+
+
+def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity: int | None = None) -> Segments:
     """Segments of occupied voxels; equals coord[mask] of masked_intersect's output
-    (model/diver.py:86-93), t = exit distance."""
+    (model/diver.py:86-93), t = exit distance.  With `capacity`: fixed-size
+    buffers, no host read (see Segments)."""
     B = _check_rays(o, v)
     m8 = _check_mask(mask, voxel_num, mask_scale)
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
+    mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), None, st)
+           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), st)
     offsets = exclusive_scan(num)
-    S, M = _totals(offsets, num)
-    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
-    t = torch.empty(S, dtype=torch.float32, device=dev)
-    ray = torch.empty(S, dtype=torch.int32, device=dev)
-    if S > 0:
+    if capacity is None:
+        S, M = _totals(offsets, num)
+    else:
+        S, M = _capacity(capacity, B, 3 * int(voxel_num)), None
+    seg, t, ray = _buffers(S, dev)
+    if S > 0 and B > 0:
         N.call("dv_masked_segments", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
                N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
-    return Segments(offsets, seg, t, ray, num, M)
+    return Segments(offsets, seg, t, ray, num, M, mx)
 
 
-def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
+def dense_segments(o, v, xyzmin, voxel_num, voxel_size, capacity: int | None = None) -> Segments:
     """Consecutive crossing points paired into segments; equals
-    (coord[:, :-1][mask], coord[:, 1:][mask]) of model/diver.py:95-103, t = entry distance."""
+    (coord[:, :-1][mask], coord[:, 1:][mask]) of model/diver.py:95-103, t = entry distance.
+    With `capacity`: fixed-size buffers, no host read (see Segments)."""
     B = _check_rays(o, v)
     dev = o.device
     st = N.stream(dev)
@@ -183,17 +215,20 @@ def dense_segments(o, v, xyzmin, voxel_num, voxel_size) -> Segments:
     pairs = torch.empty_like(num)
     N.call("dv_dense_pair_counts", B, N.ptr(num), N.ptr(pairs), st)
     offsets = exclusive_scan(pairs)
-    S, M = _totals(offsets, pairs)
-    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
-    t = torch.empty(S, dtype=torch.float32, device=dev)
-    ray = torch.empty(S, dtype=torch.int32, device=dev)
-    if S > 0:
+    mx = None
+    if capacity is None:
+        S, M = _totals(offsets, pairs)
+    else:
+        S, M = _capacity(capacity, B, 3 * int(voxel_num)), None
+        mx = pairs.max().reshape(1) if B > 0 else torch.zeros(1, dtype=torch.int32, device=dev)
+    seg, t, ray = _buffers(S, dev)
+    if S > 0 and B > 0:
         N.call("dv_dense_segments", B, float(xyzmin), float(voxel_num), float(voxel_size),
                N.ptr(o), N.ptr(v), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
-    return Segments(offsets, seg, t, ray, pairs, M)
+    return Segments(offsets, seg, t, ray, pairs, M, mx)
 
 
-def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask) -> Segments:
+def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask, capacity: int | None = None) -> Segments:
     """Occupied-voxel segments over a grid with per-axis extents: xyzmin = world
     position of corner (0,0,0) per axis, dims = (nx, ny, nz) voxels, mask
     [nz][ny][nx].  The reference supports cubic grids only; with equal values on
@@ -211,14 +246,16 @@ def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask) -> Segments:
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
+    mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o), N.ptr(v),
-           N.ptr(m8), N.ptr(num), None, st)
+           N.ptr(m8), N.ptr(num), N.ptr(mx), st)
     offsets = exclusive_scan(num)
-    S, M = _totals(offsets, num)
-    seg = torch.empty(S, 6, dtype=torch.float32, device=dev)
-    t = torch.empty(S, dtype=torch.float32, device=dev)
-    ray = torch.empty(S, dtype=torch.int32, device=dev)
-    if S > 0:
+    if capacity is None:
+        S, M = _totals(offsets, num)
+    else:
+        S, M = _capacity(capacity, B, nx + ny + nz), None
+    seg, t, ray = _buffers(S, dev)
+    if S > 0 and B > 0:
         N.call("dv_masked_segments_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o),
                N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
-    return Segments(offsets, seg, t, ray, num, M)
+    return Segments(offsets, seg, t, ray, num, M, mx)

@@ -20,7 +20,7 @@ import torch
 from torch.autograd import Function
 
 from . import _native as N
-from .decoder import Decoder, pack_plain, pack_tc, pack_tc_bwd
+from .decoder import Decoder, pack_plain, tc_index_maps
 from .ray_voxel_intersection import Segments, dense_segments, masked_segments, masked_segments_grid
 
 KIND_ID = {"diver32": 32, "diver64": 64}
@@ -61,19 +61,44 @@ def _check_params(kind: int, channels: int, params: torch.Tensor):
 
 
 class TcWeights:
-    """Decoder weights in the tensor-core operand layout (BF16 or FP16) on the device."""
+    """Decoder weights in the tensor-core operand layout (BF16 or FP16) on the
+    device.  The images are gathered from the packed plain parameters on the
+    device (`refresh`), into buffers that keep their addresses, so a refresh
+    after an optimizer step needs no host round trip and can sit inside a
+    captured CUDA graph."""
 
-    def __init__(self, decoder: Decoder, device, bf16: bool = True):
-        blob, bias, table = pack_tc(decoder, bf16)
-        self.blob = blob.to(device)
-        self.bias = bias.to(device)
-        self.table = table.contiguous()
-        self.bf16 = bool(bf16)
+    def __init__(self, kind: str, channels: int, device, bf16: bool = True):
+        maps = tc_index_maps(kind, channels)
+        self.kind, self.channels, self.bf16 = kind, channels, bool(bf16)
+        self.dtype = torch.bfloat16 if bf16 else torch.float16
+        self._i_fwd = maps["fwd"].to(device)
+        self._i_bias = maps["bias"].to(device)
+        self.table = maps["table"].contiguous()
+        self.blob = torch.zeros(self._i_fwd.numel() * 2, dtype=torch.uint8, device=device)
+        self.bias = torch.zeros(self._i_bias.numel(), dtype=torch.float32, device=device)
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.bwd = None
-        if decoder.kind == "diver32" and decoder.channels == 32 and bf16:
-            wb, tb = pack_tc_bwd(decoder, bf16)
-            self.bwd = (wb.to(device), tb.contiguous())
+        self._i_bwd = None
+        if "bwd" in maps and bf16:
+            self._i_bwd = maps["bwd"].to(device)
+            self.bwd = (torch.zeros(self._i_bwd.numel() * 2, dtype=torch.uint8, device=device),
+                        maps["bwd_table"].contiguous())
+        self.version = None
+
+    @staticmethod
+    def from_decoder(decoder: Decoder, device, bf16: bool = True) -> "TcWeights":
+        tw = TcWeights(decoder.kind, decoder.channels, device, bf16)
+        tw.refresh(pack_plain(decoder).to(device))
+        return tw
+
+    def refresh(self, params: torch.Tensor) -> None:
+        """Rebuilds the images from the packed plain parameters (device ops only)."""
+        p = params.detach().reshape(-1)
+        ext = torch.cat([p.new_zeros(1), p])
+        self.blob.view(self.dtype).copy_(ext[self._i_fwd])
+        self.bias.copy_(ext[self._i_bias])
+        if self.bwd is not None:
+            self.bwd[0].view(self.dtype).copy_(ext[self._i_bwd])
 
     def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st) -> bool:
         """Tensor-core backward (DIVeR32, BF16); False when this decoder / form
@@ -84,16 +109,16 @@ class TcWeights:
         wb, tb = self.bwd
         _timed("dv_decode_bwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), N.ptr(wb), wb.numel(), tb.data_ptr(), tb.shape[0],
-               N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, N.ptr(pe_feat), N.ptr(pe_out),
-               N.ptr(d4), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
+               N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_feat),
+               N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
         return True
 
     def decode(self, kind, channels, voxels, seg, pe_out, out4, st, voxels16=None):
         nx, ny, nz, c = _grid(voxels)
         _timed("dv_decode_fwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), N.ptr(voxels16),
-               nx, ny, nz,
-               N.ptr(seg.seg), N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(out4), N.ptr(self.err), st)
+               nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_out), N.ptr(out4),
+               N.ptr(self.err), st)
 
 
 class SegmentRender(Function):
@@ -114,17 +139,21 @@ class SegmentRender(Function):
         out4 = torch.empty(S, 4, device=dev)
         if tc is None:
             _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
-                   S, N.ptr(pe_out), N.ptr(out4), st)
+                   S, seg.count_ptr, N.ptr(pe_out), N.ptr(out4), st)
         else:
             tc.decode(kind, c, voxels, seg, pe_out, out4, st, voxels16)
         rgb = torch.empty(B, 3, device=dev)
         reg = torch.empty(B, device=dev)
         _timed("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), int(bool(white_back)), N.ptr(rgb), None,
                N.ptr(reg), st)
-        M = max(seg.max_count, 1)
-        reg_mean = reg.sum() / float(B * M)
+        # mean over the padded [B, M]; M (max segments per ray) stays on the
+        # device when the segments were built without a host read
+        M = seg.max_count if seg.max_count is not None else seg.max_dev.clamp_min(1).float()
+        if not isinstance(M, torch.Tensor):
+            M = float(max(M, 1))
+        reg_mean = reg.sum() / (float(B) * M)
         ctx.save_for_backward(voxels, params, dirs, pe_feat, pe_out, out4, rgb)
-        ctx.seg, ctx.kind, ctx.BM, ctx.tc = seg, kind, float(B * M), tc
+        ctx.seg, ctx.kind, ctx.M, ctx.tc = seg, kind, M, tc
         return rgb, reg_mean
 
     @staticmethod
@@ -136,15 +165,20 @@ class SegmentRender(Function):
         st = N.stream(dev)
         B = dirs.shape[0]
         g_rgb = (g_rgb if g_rgb is not None else torch.zeros(B, 3, device=dev)).contiguous()
-        reg_coef = float(g_reg) / ctx.BM if g_reg is not None else 0.0
+        # d reg / d sigma carries dL/dreg / (B M): 1/B on the host, dL/dreg / M
+        # as a device scalar (no host read of either)
+        scale = None
+        if g_reg is not None:
+            scale = (g_reg.detach().float().reshape(1) / ctx.M).reshape(1).contiguous()
         d4 = torch.empty_like(out4)
-        _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb), reg_coef, N.ptr(d4), st)
+        _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb),
+               1.0 / B if scale is not None else 0.0, N.ptr(scale), N.ptr(d4), st)
         gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
         if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st):
             return gv, gp, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
-               seg.total, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
+               seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
         return gv, gp, None, None, None, None, None, None
 
 
@@ -176,34 +210,44 @@ class DIVeRField(torch.nn.Module):
         self.white_back = white_back
         self.decoder = decoder
         self._tc = {}
+        self.refresh_always = False
 
     def tc_weights(self, form: str) -> TcWeights | None:
         """Tensor-core weights for form 'bf16' / 'fp16' (None for 'fp32'),
-        packed from the current decoder parameters."""
+        refreshed on the device whenever the decoder parameters changed (or on
+        every call while `refresh_always` is set, as inside a captured graph,
+        so that each replay packs the parameters of that moment)."""
         if form == "fp32":
             return None
-        from .decoder import unpack_plain_grad
-
-        key = (form, self.params._version)
-        if key not in self._tc:
-            layers = unpack_plain_grad(self.kind, self.voxels.shape[-1], self.params.detach().cpu())
-            dec = Decoder(self.kind, self.voxels.shape[-1], layers)
-            self._tc = {key: TcWeights(dec, self.voxels.device, bf16=(form == "bf16"))}
-        return self._tc[key]
+        tw = self._tc.get(form)
+        if tw is None:
+            tw = self._tc[form] = TcWeights(self.kind, self.voxels.shape[-1], self.voxels.device, form == "bf16")
+        if self.refresh_always or tw.version != self.params._version:
+            tw.refresh(self.params)
+            tw.version = self.params._version
+        return tw
 
     @staticmethod
     def from_scene(scene, device="cuda") -> "DIVeRField":
         return DIVeRField(scene.features.to(device), scene.decoder, scene.mask.to(device), scene.xyzmin,
                           scene.voxel_size, scene.mask_scale, scene.white_back)
 
-    def segments(self, os: torch.Tensor, ds: torch.Tensor) -> Segments:
+    def segment_capacity(self, batch: int) -> int:
+        """Segments that `batch` rays can produce at most: a ray crosses at most
+        nx + ny + nz + 3 grid planes, one per walk step."""
+        return batch * (sum(self.dims) + 3)
+
+    def segments(self, os: torch.Tensor, ds: torch.Tensor, capacity: int | None = None) -> Segments:
+        """CSR segments of the rays.  With `capacity` (at least
+        segment_capacity(B)) the buffers have that fixed size and the count
+        stays on the device: no host read, so the call can be captured."""
         if self.aniso:
             x0 = self.xyzmin if isinstance(self.xyzmin, tuple) else (self.xyzmin,) * 3
-            return masked_segments_grid(os, ds, x0, self.dims, self.voxel_size, self.voxel_mask)
+            return masked_segments_grid(os, ds, x0, self.dims, self.voxel_size, self.voxel_mask, capacity)
         if self.voxel_mask is not None:
             return masked_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, self.voxel_mask,
-                                   self.mask_scale)
-        return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size)
+                                   self.mask_scale, capacity)
+        return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, capacity)
 
     def grid16(self, form: str) -> torch.Tensor | None:
         """BF16/FP16 copy of the feature grid for tensor-core rendering (made
@@ -217,11 +261,12 @@ class DIVeRField(torch.nn.Module):
             self._g16key = key
         return self._g16
 
-    def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32"):
+    def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
         form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder).  Without
-        autograd the tensor-core forms read a 16-bit copy of the grid."""
-        seg = self.segments(os.contiguous(), ds.contiguous())
+        autograd the tensor-core forms read a 16-bit copy of the grid.
+        capacity: fixed segment buffers, no host synchronisation (see segments)."""
+        seg = self.segments(os.contiguous(), ds.contiguous(), capacity)
         g16 = self.grid16(form) if not torch.is_grad_enabled() else None
         return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back,
                                self.tc_weights(form), g16)

@@ -183,6 +183,10 @@ DV_API int dv_integrate_bwd(const float* grad_feature, int nvx, int nvy, int nvz
  * W^T [in][out4] (out4 = out rounded up to 4, extra columns 0) followed by the
  * bias [out4]; dv_decoder_param_count gives its length in floats.
  * Segments are the CSR lists of dv_masked_segments / dv_dense_segments.
+ * n_seg_dev (optional, device int64, e.g. offsets + batch): the decode
+ * kernels then read the segment count there, clamped to n_seg, which becomes
+ * the capacity of the segment buffers; no host read of the count is needed,
+ * so the launches can be recorded in a CUDA graph.
  * Replaces DIVeR.forward/decode/render (model/diver.py:159-207) and the
  * training loss (train.py:84-85,109-113).
  * ------------------------------------------------------------------------ */
@@ -197,7 +201,7 @@ DV_API int dv_ray_pe(int kind, int channels, const float* params, int batch, con
 /* out4 [n_seg][4] = (sigma_raw, sigmoid rgb) per segment. */
 DV_API int dv_decode_fwd(int kind, int channels, const float* params, const float* voxels, int nvx,
                          int nvy, int nvz, const float* seg, const int* seg_ray, long long n_seg,
-                         const float* pe_out, float* out4, void* stream);
+                         const int64_t* n_seg_dev, const float* pe_out, float* out4, void* stream);
 
 /* rgb [batch][3] (+ T_final if white_back), optional t_final [batch] and
  * reg_sum [batch] = sum over the ray's segments of log(1 + sigma^2 / 0.5). */
@@ -205,16 +209,19 @@ DV_API int dv_composite_fwd(int batch, const int64_t* offsets, const float* out4
                             float* rgb, float* t_final, float* reg_sum, void* stream);
 
 /* d4 [n_seg][4] = (dL/dsigma_raw, dL/drgb_seg) from grad_rgb [batch][3];
- * reg_coef multiplies d/dsigma log(1 + sigma^2/0.5). */
+ * reg_coef multiplies d/dsigma log(1 + sigma^2/0.5), and so does *reg_scale
+ * (device float, optional: a factor known only on the device, e.g.
+ * dL/dreg / max segments per ray inside a captured CUDA graph). */
 DV_API int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4, const float* rgb,
-                            const float* grad_rgb, float reg_coef, float* d4, void* stream);
+                            const float* grad_rgb, float reg_coef, const float* reg_scale, float* d4,
+                            void* stream);
 
 /* Accumulates the feature-grid gradient (grad_voxels, same layout as voxels)
  * and the packed parameter gradient (grad_params) of the segments' decode. */
 DV_API int dv_decode_bwd(int kind, int channels, const float* params, const float* voxels, int nvx,
                          int nvy, int nvz, const float* seg, const int* seg_ray, long long n_seg,
-                         const float* pe_feat, const float* pe_out, const float* d4,
-                         float* grad_voxels, float* grad_params, void* stream);
+                         const int64_t* n_seg_dev, const float* pe_feat, const float* pe_out,
+                         const float* d4, float* grad_voxels, float* grad_params, void* stream);
 
 /*
  * Tensor-core form of dv_decode_fwd: the same decoder with its matrix
@@ -231,9 +238,9 @@ DV_API int dv_decode_bwd(int kind, int channels, const float* params, const floa
 DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes,
                             const float* bias, int nbias, const int* layers, int n_layers,
                             const float* voxels, const void* voxels16, int nvx, int nvy, int nvz,
-                            const float* seg,
-                            const int* seg_ray, long long n_seg, const float* pe_out, float* out4,
-                            int* err, void* stream);
+                            const float* seg, const int* seg_ray, long long n_seg,
+                            const int64_t* n_seg_dev, const float* pe_out, float* out4, int* err,
+                            void* stream);
 
 /*
  * Allocation-free form of dv_exclusive_scan (no counterpart in the reference,
@@ -264,9 +271,9 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
                             const float* bias, int nbias, const int* f_layers, const void* wb,
                             int wb_bytes, const int* b_layers, int n_layers, const float* voxels,
                             int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
-                            long long n_seg, const float* pe_feat, const float* pe_out,
-                            const float* d4, float* grad_voxels, float* grad_params, int* err,
-                            void* stream);
+                            long long n_seg, const int64_t* n_seg_dev, const float* pe_feat,
+                            const float* pe_out, const float* d4, float* grad_voxels,
+                            float* grad_params, int* err, void* stream);
 
 /* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.

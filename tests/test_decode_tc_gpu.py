@@ -58,7 +58,7 @@ def test_tc_segments_match_fp32(kind, channels, form):
     N.call("dv_ray_pe", k, channels, N.ptr(field.params), o.shape[0], N.ptr(v), N.ptr(pe_feat), N.ptr(pe_out), st)
     ref = torch.empty(seg.total, 4, device="cuda")
     N.call("dv_decode_fwd", k, channels, N.ptr(field.params), N.ptr(field.voxels), 65, 65, 65, N.ptr(seg.seg),
-           N.ptr(seg.ray), seg.total, N.ptr(pe_out), N.ptr(ref), st)
+           N.ptr(seg.ray), seg.total, None, N.ptr(pe_out), N.ptr(ref), st)
     tcw = field.tc_weights(form)
     scale = ref.abs().max(0).values.cpu().numpy()
     # FP32 grid rows, then the 16-bit copy of the grid used for rendering
@@ -109,7 +109,7 @@ def test_tc_backward_matches_fp32_backward(form, golden):
     for f in ("fp32", form):
         vox = torch.from_numpy(g["voxels"]).cuda().requires_grad_(True)
         params = pack_plain(dec).cuda().requires_grad_(True)
-        tc = None if f == "fp32" else TcWeights(dec, "cuda", bf16=(f == "bf16"))
+        tc = None if f == "fp32" else TcWeights.from_decoder(dec, "cuda", bf16=(f == "bf16"))
         rgb, reg = render_segments(vox, params, seg, d, "diver32", True, tc)
         (torch.nn.functional.mse_loss(rgb, tgt) + 1e-5 * reg).backward()
         torch.cuda.synchronize()
