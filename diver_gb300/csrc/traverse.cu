@@ -193,6 +193,15 @@ struct SegWriter {
 
 // Masked walk: (entry, exit) of every voxel whose occupancy byte is set.
 // Reference ray_voxel_intersect.cu:203-318.
+//
+// The crossing points form a dependent chain, but the occupancy byte of a
+// voxel only decides whether its segment is recorded.  The walk therefore
+// runs LOOKAHEAD steps ahead: it computes up to LOOKAHEAD crossings and issues
+// their occupancy loads back to back, then records the occupied ones in
+// order, so a ray waits for one load latency per LOOKAHEAD voxels instead of
+// one per voxel (which bounds small batches, where few warps are resident).
+constexpr int LOOKAHEAD = 8;
+
 template <int MODE, bool FAST>
 __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, const float3 d, float t) {
   const float3 s = signs(d);
@@ -210,29 +219,53 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
   }
   SegWriter w;
   int count = 0;
-  float3 q;
-  float dt;
-  while (true) {
-    grid_step<FAST>(p, d, r, s, q, dt);
-    t = __fadd_rn(t, dt);
-    if (outside_closed3(q, a.n3)) break;
-    const long long idx = cell_index3(p, q, a.mask_scale, a.mx, a.my);
-    if (occupied(a.mask, idx, a.cells)) {
-      if (MODE == WALK_PADDED && count < a.max_n) {
-        float* rr = row + 6 * count;
-        rr[0] = p.x;
-        rr[1] = p.y;
-        rr[2] = p.z;
-        rr[3] = q.x;
-        rr[4] = q.y;
-        rr[5] = q.z;
-        trow[count] = __fmul_rn(t, a.voxel_size);
+  bool done = false;
+  while (!done) {
+    float3 P[LOOKAHEAD + 1];
+    float T[LOOKAHEAD];
+    uint8_t occ[LOOKAHEAD];
+    unsigned inb = 0;  // bit k: step k stayed in the box and its cell is inside the mask
+    P[0] = p;
+#pragma unroll
+    for (int k = 0; k < LOOKAHEAD; ++k) {
+      if (!done) {
+        float3 q;
+        float dt;
+        grid_step<FAST>(P[k], d, r, s, q, dt);
+        t = __fadd_rn(t, dt);
+        if (outside_closed3(q, a.n3)) {
+          done = true;
+        } else {
+          P[k + 1] = q;
+          T[k] = t;
+          const long long idx = cell_index3(P[k], q, a.mask_scale, a.mx, a.my);
+          const bool in_mask = idx >= 0 && idx < a.cells;
+          // the address is clamped rather than the loaded value selected, so
+          // nothing reads the byte before all LOOKAHEAD loads are in flight
+          occ[k] = __ldg(a.mask + (in_mask ? idx : 0));
+          inb |= (in_mask ? 1u : 0u) << k;
+        }
       }
-      if (MODE == WALK_SEGMENTS && count < cap)
-        w.put(a, b, base + count, count + 1 < cap, p, q, __fmul_rn(t, a.voxel_size));
-      ++count;
     }
-    p = q;
+#pragma unroll
+    for (int k = 0; k < LOOKAHEAD; ++k) {
+      if (((inb >> k) & 1u) && occ[k] != 0) {
+        if (MODE == WALK_PADDED && count < a.max_n) {
+          float* rr = row + 6 * count;
+          rr[0] = P[k].x;
+          rr[1] = P[k].y;
+          rr[2] = P[k].z;
+          rr[3] = P[k + 1].x;
+          rr[4] = P[k + 1].y;
+          rr[5] = P[k + 1].z;
+          trow[count] = __fmul_rn(T[k], a.voxel_size);
+        }
+        if (MODE == WALK_SEGMENTS && count < cap)
+          w.put(a, b, base + count, count + 1 < cap, P[k], P[k + 1], __fmul_rn(T[k], a.voxel_size));
+        ++count;
+      }
+    }
+    p = P[LOOKAHEAD];  // only read again when all LOOKAHEAD steps stayed inside
   }
   if (MODE == WALK_SEGMENTS) w.flush(a, b);
   return count;
