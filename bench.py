@@ -170,33 +170,9 @@ def train_scene(device):
 def make_batches(scene, count, device, seed=4):
     """`count` batches of BATCH rays from 100 cameras at 800x800 (focal 960),
     kept only where the ray crosses at least one occupied voxel."""
-    import torch
-
-    from diver_gb300 import _native as N
     from diver_gb300 import scenes
 
-    cams = scenes.sphere_cameras(100, 4.0, 3)
-    dirs_cam = scenes.pixel_directions(800, 800, 960.0, device).reshape(-1, 3)
-    g = torch.Generator(device=device).manual_seed(seed)
-    gc = torch.Generator().manual_seed(seed)
-    out = []
-    m8 = scene.mask.view(torch.uint8)
-    while len(out) < count:
-        c2w = cams[int(torch.randint(0, 100, (1,), generator=gc))].to(device)
-        pick = torch.randint(0, dirs_cam.shape[0], (3 * BATCH,), generator=g, device=device)
-        d = dirs_cam[pick] @ c2w[:, :3].t()
-        d = (d / d.norm(dim=-1, keepdim=True)).contiguous()
-        o = c2w[:, 3].expand(d.shape).contiguous()
-        num = torch.empty(d.shape[0], dtype=torch.int32, device=device)
-        N.call("dv_masked_count", d.shape[0], scene.xyzmin, float(scene.voxel_num), scene.voxel_size, 1.0,
-               N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, N.stream(device))
-        keep = torch.nonzero(num > 0)[:, 0]
-        if keep.numel() < BATCH:
-            continue
-        keep = keep[:BATCH]
-        tgt = torch.rand(BATCH, 3, generator=g, device=device)
-        out.append((o[keep].contiguous(), d[keep].contiguous(), tgt))
-    return out
+    return scenes.training_batches(scene, count, BATCH, device, seed)
 
 
 def train_step(field, o, d, tgt, form="fp32"):

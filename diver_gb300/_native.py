@@ -45,9 +45,11 @@ SIGNATURES = {
     "dv_composite_fwd": (I32, [I32, P, P, I32, P, P, P, P]),
     "dv_composite_bwd": (I32, [I32, P, P, P, P, F32, P, P, P]),
     "dv_decode_bwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, P, P, P]),
-    "dv_decode_fwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, P]),
+    "dv_decode_fwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, I64, P,
+                               P]),
+    "dv_decode_tc_save_bytes": (I64, [I32, I32, I64]),
     "dv_decode_bwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, P, I32, P, I32, P, I32, I32, I32, P, P, I64, P, P,
-                               P, P, P, P, P, P]),
+                               P, P, P, I64, P, P, P, P, P]),
     "dv_realtime_packed_size": (I32, [I32]),
     "dv_realtime_pack": (I32, [I32, P, P, P]),
     "dv_mlp_eval": (I32, [I32, I32, P, P, P, I32, P, P, P, P, P]),

@@ -49,6 +49,9 @@ struct TcArgs {
   int nbias;   // multiple of 4
   TcLayer L[TC_MAX_LAYERS];
   int* err;    // set to 1 if an MMA completion wait timed out
+  uint8_t* save;       // optional: every layer's input tile, per 128-segment tile (training)
+  int save_off[TC_MAX_LAYERS];  // byte offset of layer l's input tile inside a tile's record
+  int save_bytes;      // bytes per tile record (sum of 256 * K over the layers)
 };
 
 template <int C, int BF16>
@@ -127,11 +130,18 @@ __device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long S, lon
 }
 
 // Issues one layer's MMA chain (thread 0) and waits for it (all threads).
+// With `save`, thread 0 also copies the layer's input tile (the A operand,
+// 256 * K bytes) to global memory by a bulk async copy and, before the
+// caller's barrier lets anyone overwrite A, waits until that copy has read it.
 template <int BF16>
 __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, const uint8_t* sA, uint32_t tmem,
-                                         uint64_t* bar, uint32_t& phase) {
+                                         uint64_t* bar, uint32_t& phase, uint8_t* save = nullptr) {
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
+    if (save != nullptr) {
+      tc::bulk_store(save, sA, (uint32_t)L.K * 256u);
+      tc::bulk_commit();
+    }
     const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
     const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB + L.b_off);
     const uint32_t sbo = (uint32_t)(L.K / 8) * 128;
@@ -143,6 +153,7 @@ __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, co
   const bool done = tc::mbar_wait_bounded(bar, phase);
   phase ^= 1u;
   tc::fence_after_sync();
+  if (save != nullptr && threadIdx.x == 0) tc::bulk_wait_read();
   return done;
 }
 
@@ -200,6 +211,8 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     const long long s0 = tile * 128;
     const long long s = s0 + t;
     const bool valid = s < S;
+    uint8_t* rec = a.save ? a.save + tile * (long long)a.save_bytes : nullptr;
+#define DV_SAVE(l) (rec ? rec + a.save_off[l] : nullptr)
     if (a.grid16)
       gather_tile_16<C, BF16>(a, S, s0, sA);
     else
@@ -209,7 +222,7 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     // mlp1 hidden layers: D = relu(A W^T + b)
 #pragma unroll 1
     for (int l = 0; l < D1 && ok; ++l) {
-      ok = tc_layer<BF16>(a.L[l], sB, sA, tmem, bar, phase);
+      ok = tc_layer<BF16>(a.L[l], sB, sA, tmem, bar, phase, DV_SAVE(l));
       ok = __syncthreads_and(ok);
       if (!ok) break;
 #pragma unroll
@@ -224,7 +237,7 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     }
     if (!ok) break;
     // mlp1 output: columns 0..W-1 hidden (no activation), column W sigma
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1], sB, sA, tmem, bar, phase));
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1], sB, sA, tmem, bar, phase, DV_SAVE(D1)));
     if (!ok) break;
     float sigma;
     {
@@ -243,7 +256,7 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     }
     sync_for_mma();
     // mlp2 first layer: relu(hidden W^T + per-ray (bias + PE term))
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 1], sB, sA, tmem, bar, phase));
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 1], sB, sA, tmem, bar, phase, DV_SAVE(D1 + 1)));
     if (!ok) break;
     {
       const int ray = valid ? __ldg(a.seg_ray + s) : 0;
@@ -265,7 +278,8 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     }
     sync_for_mma();
     // mlp2 output: 3 logits -> sigmoid
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 2], sB, sA, tmem, bar, phase));
+    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 2], sB, sA, tmem, bar, phase, DV_SAVE(D1 + 2)));
+#undef DV_SAVE
     if (!ok) break;
     {
       float o[4];
@@ -280,6 +294,7 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     __syncthreads();  // the next gather overwrites A
   }
   if (!ok && t == 0 && a.err) atomicExch(a.err, 1);
+  if (a.save != nullptr && t == 0) tc::bulk_wait_all();
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -323,7 +338,8 @@ extern "C" {
 int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
                      const int* layers, int n_layers, const float* voxels, const void* voxels16, int nvx, int nvy,
                      int nvz, const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
-                     const float* pe_out, float* out4, int* err, void* stream) {
+                     const float* pe_out, float* out4, void* save, long long save_capacity, int* err,
+                     void* stream) {
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
   const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
   DV_CHECK(d1 > 0 && n_layers == d1 + 3 && n_layers <= TC_MAX_LAYERS, DV_ERR_ARG);
@@ -362,6 +378,18 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
     DV_CHECK((long long)L.b_off + (long long)L.N * L.K * 2 <= wbytes && L.bias_off + L.N <= nbias, DV_ERR_ARG);
     DV_CHECK(L.N <= (W == 32 ? 64 : 128), DV_ERR_ARG);
   }
+  // saved layer inputs: one record of sum(256 K) bytes per 128-segment tile
+  if (save != nullptr) {
+    int off = 0;
+    for (int l = 0; l < n_layers; ++l) {
+      a.save_off[l] = off;
+      off += 256 * a.L[l].K;
+    }
+    a.save = reinterpret_cast<uint8_t*>(save);
+    a.save_bytes = off;
+    DV_CHECK(((uintptr_t)save & 15) == 0, DV_ERR_ARG);
+    DV_CHECK((n_seg + 127) / 128 * (long long)off <= save_capacity, DV_ERR_ARG);
+  }
   // layer shapes the kernel assumes
   DV_CHECK(a.L[0].K == channels && a.L[0].N == W, DV_ERR_ARG);
   for (int l = 1; l < d1; ++l) DV_CHECK(a.L[l].K == W && a.L[l].N == W, DV_ERR_ARG);
@@ -372,6 +400,13 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
   if (channels == 32)
     return bf16 ? launch_decode_fwd_tc<32, 64, 1, 1>(a, st) : launch_decode_fwd_tc<32, 64, 1, 0>(a, st);
   return bf16 ? launch_decode_fwd_tc<64, 64, 1, 1>(a, st) : launch_decode_fwd_tc<64, 64, 1, 0>(a, st);
+}
+
+long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg) {
+  const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
+  if (d1 < 0 || n_seg < 0) return -1;
+  const long long record = 256LL * (channels + (d1 + 2) * kind);
+  return (n_seg + 127) / 128 * record;
 }
 
 }  // extern "C"

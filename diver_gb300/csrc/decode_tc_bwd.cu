@@ -63,7 +63,13 @@ struct Args {
   int f_off[NL], f_K[NL], f_N[NL], f_bias[NL];  // forward layer table
   int b_off_img[NL], b_K[NL], b_N[NL];          // backward layer table
   int* err;
+  // optional: the forward's saved layer inputs (dv_decode_fwd_tc's save
+  // records: X0, A1, A2, hidden, A4 tiles, 8 KiB each) and its out4; then the
+  // corner rows are not gathered and the forward is not recomputed
+  const uint8_t* saved;
+  const float4* out4;
 };
+constexpr uint32_t SAVE_TILE = 128 * 2 * (C + 4 * W);  // bytes of one saved record
 
 struct Smem {
   uint8_t *Bf, *Bb;
@@ -71,6 +77,7 @@ struct Smem {
   uint8_t *X0, *A1, *A2, *HP, *A4, *D;
   float* stage;  // fp32 [128][C+4], aliases A1..HP
   uint64_t* bar;
+  uint64_t* bar_load;  // completion of the bulk loads of saved tiles
   uint32_t* tslot;
 };
 
@@ -172,7 +179,8 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   m.D = p;
   p += 128 * FD * 2;
   m.bar = reinterpret_cast<uint64_t*>(p);
-  m.tslot = reinterpret_cast<uint32_t*>(p + 8);
+  m.bar_load = reinterpret_cast<uint64_t*>(p + 8);
+  m.tslot = reinterpret_cast<uint32_t*>(p + 16);
 
   const int t = threadIdx.x, warp = t >> 5;
   for (int i = t; i < a.wf_bytes / 16; i += 128)
@@ -184,6 +192,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   for (int i = t; i < 128 * FH * 2 / 16; i += 128) reinterpret_cast<uint4*>(m.HP)[i] = make_uint4(0, 0, 0, 0);
   if (t == 0) {
     tc::mbar_init(m.bar, 1);
+    tc::mbar_init(m.bar_load, 1);
     tc::fence_mbar_init();
   }
   if (warp == 0) {
@@ -195,7 +204,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
   const uint32_t tmem = *m.tslot;
   const uint32_t lane = (uint32_t)(warp * 32) << 16;
   const uint32_t trow = tmem + lane;
-  uint32_t phase = 0;
+  uint32_t phase = 0, phase_load = 0;
   bool ok = true, first = true;
   float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
   float v[48];
@@ -207,117 +216,160 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
     const long long s = s0 + t;
     const bool valid = s < S;
     const int ray = valid ? __ldg(a.seg_ray + s) : 0;
-    // ---- gather: feature rows ----
-    {
-      constexpr int TPS = C / 4, SPP = 128 / TPS;
-#pragma unroll 1
-      for (int pp = 0; pp < TPS; ++pp) {
-        const int ls = pp * SPP + t / TPS, q = t % TPS;
-        const long long ss = s0 + ls;
-        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ss < S) {
-          const float* sg = a.seg + ss * 6;
-          const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3),
-                                               __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
-          f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
+    if (a.saved != nullptr) {
+      // ---- saved layer inputs: bulk copies into X0, A1, A2, HP (hidden half), A4 ----
+      sync_mma();  // the previous tile's reads of these buffers (and of the staging alias) are done
+      if (t == 0) {
+        const uint8_t* rec = a.saved + tile * (long long)SAVE_TILE;
+        tc::mbar_arrive_expect_tx(m.bar_load, SAVE_TILE);
+        tc::bulk_load(m.X0, rec, 128 * C * 2, m.bar_load);
+        rec += 128 * C * 2;
+        tc::bulk_load(m.A1, rec, 128 * W * 2, m.bar_load);
+        tc::bulk_load(m.A2, rec + 128 * W * 2, 128 * W * 2, m.bar_load);
+        rec += 2 * 128 * W * 2;
+        // hidden tile [128][W] -> columns 0..W-1 of HP [128][FH]: one copy per 8-row group
+        for (int gi = 0; gi < 16; ++gi)
+          tc::bulk_load(m.HP + gi * (FH / 8) * 128, rec + gi * (W / 8) * 128, (W / 8) * 128, m.bar_load);
+        rec += 128 * W * 2;
+        tc::bulk_load(m.A4, rec, 128 * W * 2, m.bar_load);
+      }
+      {
+        const float4* pf = reinterpret_cast<const float4*>(a.pe_feat + (long long)ray * PE_PAD);
+#pragma unroll
+        for (int k = 0; k < PE_PAD / 4; ++k) {
+          const float4 x = __ldg(pf + k);
+          v[4 * k] = x.x;
+          v[4 * k + 1] = x.y;
+          v[4 * k + 2] = x.z;
+          v[4 * k + 3] = x.w;
         }
-        *reinterpret_cast<uint2*>(m.X0 + tc::kmajor_offset(ls, 4 * q, C)) =
-            make_uint2(tc::pack2<1>(f.x, f.y), tc::pack2<1>(f.z, f.w));
+        v[28] = v[29] = v[30] = v[31] = 0.f;
+        put_row(m.HP, FH, t, v, 32, W);
       }
-    }
-    sync_mma();
-    // ---- forward (activations kept) ----
-    if (t == 0) {
-      tc::fence_after_sync();
-      mma_rows(tmem, m.X0, C, m.Bf + a.f_off[0], C, W);
-      tc::mma_commit(m.bar);
-    }
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    tc::ld_32x32b_x32(trow, v);
-    tc::ld_wait();
-#pragma unroll
-    for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[0] + i], 0.f);
-    put_row(m.A1, W, t, v, W);
-    sync_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      mma_rows(tmem, m.A1, W, m.Bf + a.f_off[1], W, W);
-      tc::mma_commit(m.bar);
-    }
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    tc::ld_32x32b_x32(trow, v);
-    tc::ld_wait();
-#pragma unroll
-    for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[1] + i], 0.f);
-    put_row(m.A2, W, t, v, W);
-    sync_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      mma_rows(tmem, m.A2, W, m.Bf + a.f_off[2], W, W + 16);
-      tc::mma_commit(m.bar);
-    }
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    tc::ld_32x32b_x32(trow, v);
-    tc::ld_wait();
-#pragma unroll
-    for (int i = 0; i < W; ++i) v[i] += m.bias[a.f_bias[2] + i];
-    put_row(m.HP, FH, t, v, W);
-    {
-      const float4* pf = reinterpret_cast<const float4*>(a.pe_feat + (long long)ray * PE_PAD);
-#pragma unroll
-      for (int k = 0; k < PE_PAD / 4; ++k) {
-        const float4 x = __ldg(pf + k);
-        v[4 * k] = x.x;
-        v[4 * k + 1] = x.y;
-        v[4 * k + 2] = x.z;
-        v[4 * k + 3] = x.w;
+      ok = __syncthreads_and(tc::mbar_wait_bounded(m.bar_load, phase_load));
+      phase_load ^= 1u;
+      if (!ok) break;
+    } else {
+      // ---- gather: feature rows ----
+      {
+        constexpr int TPS = C / 4, SPP = 128 / TPS;
+  #pragma unroll 1
+        for (int pp = 0; pp < TPS; ++pp) {
+          const int ls = pp * SPP + t / TPS, q = t % TPS;
+          const long long ss = s0 + ls;
+          float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (ss < S) {
+            const float* sg = a.seg + ss * 6;
+            const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3),
+                                                 __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
+            f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
+          }
+          *reinterpret_cast<uint2*>(m.X0 + tc::kmajor_offset(ls, 4 * q, C)) =
+              make_uint2(tc::pack2<1>(f.x, f.y), tc::pack2<1>(f.z, f.w));
+        }
       }
-      v[28] = v[29] = v[30] = v[31] = 0.f;
-      put_row(m.HP, FH, t, v, 32, W);
-    }
-    sync_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      mma_rows(tmem, m.HP, FH, m.Bf + a.f_off[3], W, W);  // hidden columns only (K = W)
-      tc::mma_commit(m.bar);
-    }
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
-    tc::ld_32x32b_x32(trow, v);
-    tc::ld_wait();
-    {
-      const float4* po = reinterpret_cast<const float4*>(a.pe_out + (long long)ray * W);
-#pragma unroll
-      for (int i = 0; i < W; i += 4) {
-        const float4 x = __ldg(po + i / 4);
-        v[i] = fmaxf(v[i] + x.x, 0.f);
-        v[i + 1] = fmaxf(v[i + 1] + x.y, 0.f);
-        v[i + 2] = fmaxf(v[i + 2] + x.z, 0.f);
-        v[i + 3] = fmaxf(v[i + 3] + x.w, 0.f);
+      sync_mma();
+      // ---- forward (activations kept) ----
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_rows(tmem, m.X0, C, m.Bf + a.f_off[0], C, W);
+        tc::mma_commit(m.bar);
       }
+      ok = __syncthreads_and(wait_mma(m.bar, phase));
+      if (!ok) break;
+      tc::ld_32x32b_x32(trow, v);
+      tc::ld_wait();
+  #pragma unroll
+      for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[0] + i], 0.f);
+      put_row(m.A1, W, t, v, W);
+      sync_mma();
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_rows(tmem, m.A1, W, m.Bf + a.f_off[1], W, W);
+        tc::mma_commit(m.bar);
+      }
+      ok = __syncthreads_and(wait_mma(m.bar, phase));
+      if (!ok) break;
+      tc::ld_32x32b_x32(trow, v);
+      tc::ld_wait();
+  #pragma unroll
+      for (int i = 0; i < W; ++i) v[i] = fmaxf(v[i] + m.bias[a.f_bias[1] + i], 0.f);
+      put_row(m.A2, W, t, v, W);
+      sync_mma();
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_rows(tmem, m.A2, W, m.Bf + a.f_off[2], W, W + 16);
+        tc::mma_commit(m.bar);
+      }
+      ok = __syncthreads_and(wait_mma(m.bar, phase));
+      if (!ok) break;
+      tc::ld_32x32b_x32(trow, v);
+      tc::ld_wait();
+  #pragma unroll
+      for (int i = 0; i < W; ++i) v[i] += m.bias[a.f_bias[2] + i];
+      put_row(m.HP, FH, t, v, W);
+      {
+        const float4* pf = reinterpret_cast<const float4*>(a.pe_feat + (long long)ray * PE_PAD);
+  #pragma unroll
+        for (int k = 0; k < PE_PAD / 4; ++k) {
+          const float4 x = __ldg(pf + k);
+          v[4 * k] = x.x;
+          v[4 * k + 1] = x.y;
+          v[4 * k + 2] = x.z;
+          v[4 * k + 3] = x.w;
+        }
+        v[28] = v[29] = v[30] = v[31] = 0.f;
+        put_row(m.HP, FH, t, v, 32, W);
+      }
+      sync_mma();
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_rows(tmem, m.HP, FH, m.Bf + a.f_off[3], W, W);  // hidden columns only (K = W)
+        tc::mma_commit(m.bar);
+      }
+      ok = __syncthreads_and(wait_mma(m.bar, phase));
+      if (!ok) break;
+      tc::ld_32x32b_x32(trow, v);
+      tc::ld_wait();
+      {
+        const float4* po = reinterpret_cast<const float4*>(a.pe_out + (long long)ray * W);
+  #pragma unroll
+        for (int i = 0; i < W; i += 4) {
+          const float4 x = __ldg(po + i / 4);
+          v[i] = fmaxf(v[i] + x.x, 0.f);
+          v[i + 1] = fmaxf(v[i + 1] + x.y, 0.f);
+          v[i + 2] = fmaxf(v[i + 2] + x.z, 0.f);
+          v[i + 3] = fmaxf(v[i + 3] + x.w, 0.f);
+        }
+      }
+      put_row(m.A4, W, t, v, W);
+      sync_mma();
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_rows(tmem, m.A4, W, m.Bf + a.f_off[4], W, 16);
+        tc::mma_commit(m.bar);
+      }
+      ok = __syncthreads_and(wait_mma(m.bar, phase));
+      if (!ok) break;
     }
-    put_row(m.A4, W, t, v, W);
-    sync_mma();
-    if (t == 0) {
-      tc::fence_after_sync();
-      mma_rows(tmem, m.A4, W, m.Bf + a.f_off[4], W, 16);
-      tc::mma_commit(m.bar);
-    }
-    ok = __syncthreads_and(wait_mma(m.bar, phase));
-    if (!ok) break;
     const float4 g = valid ? a.d4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     {
-      float o[4];
-      tc::ld_32x32b_x4(trow, o);
-      tc::ld_wait();
+      float c0, c1, c2;
+      if (a.saved != nullptr) {
+        const float4 oc = valid ? a.out4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+        c0 = oc.y;
+        c1 = oc.z;
+        c2 = oc.w;
+      } else {
+        float o[4];
+        tc::ld_32x32b_x4(trow, o);
+        tc::ld_wait();
+        c0 = sigmoidf_acc(o[0] + m.bias[a.f_bias[4]]);
+        c1 = sigmoidf_acc(o[1] + m.bias[a.f_bias[4] + 1]);
+        c2 = sigmoidf_acc(o[2] + m.bias[a.f_bias[4] + 2]);
+      }
 #pragma unroll
       for (int i = 0; i < 16; ++i) v[i] = 0.f;
-      const float c0 = sigmoidf_acc(o[0] + m.bias[a.f_bias[4]]);
-      const float c1 = sigmoidf_acc(o[1] + m.bias[a.f_bias[4] + 1]);
-      const float c2 = sigmoidf_acc(o[2] + m.bias[a.f_bias[4] + 2]);
       v[0] = g.y * c0 * (1.f - c0);
       v[1] = g.z * c1 * (1.f - c1);
       v[2] = g.w * c2 * (1.f - c2);
@@ -461,7 +513,7 @@ __global__ void __launch_bounds__(128) decode_bwd_tc_kernel(const Args a) {
 
 inline size_t smem_bytes(const Args& a) {
   return (size_t)a.wf_bytes + a.wb_bytes + a.nbias * 4 + 128 * C * 2 + 2 * 128 * W * 2 + 128 * FH * 2 +
-         128 * W * 2 + 128 * FD * 2 + 16;
+         128 * W * 2 + 128 * FD * 2 + 32;
 }
 
 }  // namespace bw
@@ -476,7 +528,8 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
                      const int* f_layers, const void* wb, int wb_bytes, const int* b_layers, int n_layers,
                      const float* voxels, int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
                      long long n_seg, const int64_t* n_seg_dev, const float* pe_feat, const float* pe_out,
-                     const float* d4, float* grad_voxels, float* grad_params, int* err, void* stream) {
+                     const float* d4, const void* saved, long long saved_bytes, const float* out4,
+                     float* grad_voxels, float* grad_params, int* err, void* stream) {
   using namespace dv::bw;
   DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
   DV_CHECK(kind == 32 && channels == 32 && n_layers == NL && bf16 == 1, DV_ERR_UNSUPPORTED);
@@ -488,7 +541,13 @@ int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_by
   DV_CHECK(((uintptr_t)wf & 15) == 0 && ((uintptr_t)wb & 15) == 0 && ((uintptr_t)voxels & 15) == 0 &&
                ((uintptr_t)grad_voxels & 15) == 0 && ((uintptr_t)d4 & 15) == 0,
            DV_ERR_ARG);
+  if (saved != nullptr) {
+    DV_CHECK(out4 != nullptr && ((uintptr_t)saved & 15) == 0 && ((uintptr_t)out4 & 15) == 0, DV_ERR_ARG);
+    DV_CHECK((n_seg + 127) / 128 * (long long)SAVE_TILE <= saved_bytes, DV_ERR_ARG);
+  }
   Args a{};
+  a.saved = reinterpret_cast<const uint8_t*>(saved);
+  a.out4 = reinterpret_cast<const float4*>(out4);
   a.grid = voxels;
   a.nvx = nvx;
   a.nvy = nvy;

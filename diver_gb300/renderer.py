@@ -100,9 +100,19 @@ class TcWeights:
         if self.bwd is not None:
             self.bwd[0].view(self.dtype).copy_(ext[self._i_bwd])
 
-    def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st) -> bool:
+    def save_buffer(self, kind: int, channels: int, n_seg: int, device) -> torch.Tensor | None:
+        """Buffer for the forward's layer inputs, read back by the tensor-core
+        backward (None when this decoder / form has no tensor-core backward)."""
+        if self.bwd is None:
+            return None
+        n = int(N.lib().dv_decode_tc_save_bytes(kind, channels, n_seg))
+        return torch.empty(max(n, 16), dtype=torch.uint8, device=device)
+
+    def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st, saved=None, out4=None) -> bool:
         """Tensor-core backward (DIVeR32, BF16); False when this decoder / form
-        has none (the caller then runs the FP32 CUDA backward)."""
+        has none (the caller then runs the FP32 CUDA backward).  With `saved`
+        (the forward's save buffer) and its `out4` the forward is read back
+        instead of recomputed."""
         if self.bwd is None:
             return False
         nx, ny, nz, c = _grid(voxels)
@@ -110,15 +120,16 @@ class TcWeights:
         _timed("dv_decode_bwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), N.ptr(wb), wb.numel(), tb.data_ptr(), tb.shape[0],
                N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_feat),
-               N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
+               N.ptr(pe_out), N.ptr(d4), N.ptr(saved), 0 if saved is None else saved.numel(),
+               N.ptr(out4 if saved is not None else None), N.ptr(gv), N.ptr(gp), N.ptr(self.err), st)
         return True
 
-    def decode(self, kind, channels, voxels, seg, pe_out, out4, st, voxels16=None):
+    def decode(self, kind, channels, voxels, seg, pe_out, out4, st, voxels16=None, save=None):
         nx, ny, nz, c = _grid(voxels)
         _timed("dv_decode_fwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), N.ptr(voxels16),
                nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_out), N.ptr(out4),
-               N.ptr(self.err), st)
+               N.ptr(save), 0 if save is None else save.numel(), N.ptr(self.err), st)
 
 
 class SegmentRender(Function):
@@ -141,7 +152,10 @@ class SegmentRender(Function):
             _timed("dv_decode_fwd", kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                    S, seg.count_ptr, N.ptr(pe_out), N.ptr(out4), st)
         else:
-            tc.decode(kind, c, voxels, seg, pe_out, out4, st, voxels16)
+            # training: keep the layer inputs for the tensor-core backward
+            save = tc.save_buffer(kind, c, S, dev) if (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]) else None
+            tc.decode(kind, c, voxels, seg, pe_out, out4, st, voxels16, save)
+            ctx.saved_layers = save
         rgb = torch.empty(B, 3, device=dev)
         reg = torch.empty(B, device=dev)
         _timed("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), int(bool(white_back)), N.ptr(rgb), None,
@@ -175,7 +189,8 @@ class SegmentRender(Function):
                1.0 / B if scale is not None else 0.0, N.ptr(scale), N.ptr(d4), st)
         gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
-        if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st):
+        if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st,
+                                                  getattr(ctx, "saved_layers", None), out4):
             return gv, gp, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)

@@ -233,14 +233,23 @@ DV_API int dv_decode_bwd(int kind, int channels, const float* params, const floa
  * optional) is set to 1 if a bounded wait for an MMA ran out.  voxels16
  * (optional, may be NULL): a copy of the grid in the operand format (BF16
  * when bf16 = 1, else FP16), same layout; when given, the corner rows are read
- * from it (half the bytes) and integrated in FP32.
+ * from it (half the bytes) and integrated in FP32.  save (optional, 16-byte
+ * aligned, save_capacity bytes >= dv_decode_tc_save_bytes): receives the
+ * layer inputs for dv_decode_bwd_tc.
  */
 DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes,
                             const float* bias, int nbias, const int* layers, int n_layers,
                             const float* voxels, const void* voxels16, int nvx, int nvy, int nvz,
                             const float* seg, const int* seg_ray, long long n_seg,
-                            const int64_t* n_seg_dev, const float* pe_out, float* out4, int* err,
-                            void* stream);
+                            const int64_t* n_seg_dev, const float* pe_out, float* out4, void* save,
+                            long long save_capacity, int* err, void* stream);
+
+/* Bytes of the `save` buffer of dv_decode_fwd_tc for n_seg segments: per
+ * tile of 128 segments, every layer's input tile (BF16/FP16, the K-major
+ * operand layout) in layer order; dv_decode_bwd_tc reads them back instead
+ * of gathering the corner rows and recomputing the forward.  No counterpart
+ * in the reference (its backward is torch autograd over stored activations). */
+DV_API long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg);
 
 /*
  * Allocation-free form of dv_exclusive_scan (no counterpart in the reference,
@@ -266,13 +275,17 @@ DV_API int dv_exclusive_scan_static(const int* counts, long long n, int64_t* off
  * [N = in][K = out padded to 16] per layer (b_layers: HOST rows of
  * (byte offset, K, N)); weight gradients accumulate in FP32 from BF16/FP16
  * activations and deltas.  Returns DV_ERR_UNSUPPORTED for other decoders.
+ * saved (optional, with saved_bytes and the forward's out4): the save buffer
+ * that dv_decode_fwd_tc filled for the same segments and weights; the
+ * forward is then read back instead of recomputed (same bits).
  */
 DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, int wf_bytes,
                             const float* bias, int nbias, const int* f_layers, const void* wb,
                             int wb_bytes, const int* b_layers, int n_layers, const float* voxels,
                             int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
                             long long n_seg, const int64_t* n_seg_dev, const float* pe_feat,
-                            const float* pe_out, const float* d4, float* grad_voxels,
+                            const float* pe_out, const float* d4, const void* saved,
+                            long long saved_bytes, const float* out4, float* grad_voxels,
                             float* grad_params, int* err, void* stream);
 
 /* ------------------------------------------------------------------------

@@ -137,3 +137,47 @@ def test_tc_backward_on_the_small_scene_runs_full_tiles():
         out[form] = (field.voxels.grad.clone(), field.params.grad.clone())
     for a, b in zip(out["bf16"], out["fp32"]):
         assert ((a - b).norm() / b.norm()).item() <= TOL_GRAD["bf16"]
+
+
+def test_tc_backward_from_saved_layers_matches_recompute():
+    """The forward's saved layer inputs reproduce the recomputed forward: the
+    two backward modes agree to FP32 atomic-accumulation order (1e-6 of the
+    largest gradient magnitude)."""
+    from diver_gb300 import _native as N
+    from diver_gb300.renderer import KIND_ID
+
+    sc, o, v, field = small()
+    sc.decoder.layers[sc.decoder.n_mlp1 - 1][1][0] += 0.6
+    from diver_gb300.renderer import DIVeRField
+
+    field = DIVeRField.from_scene(sc, "cuda")
+    o, v = o.cuda(), v.cuda()
+    seg = field.segments(o, v)
+    k, C, B, S = KIND_ID["diver32"], 32, o.shape[0], seg.total
+    st = N.stream()
+    tw = field.tc_weights("bf16")
+    pe_feat = torch.empty(B, 28, device="cuda")
+    pe_out = torch.empty(B, 32, device="cuda")
+    N.call("dv_ray_pe", k, C, N.ptr(field.params), B, N.ptr(v), N.ptr(pe_feat), N.ptr(pe_out), st)
+    out4 = torch.empty(S, 4, device="cuda")
+    save = tw.save_buffer(k, C, S, "cuda")
+    tw.decode(k, C, field.voxels, seg, pe_out, out4, st, None, save)
+    out4_ref = torch.empty_like(out4)
+    tw.decode(k, C, field.voxels, seg, pe_out, out4_ref, st)
+    assert torch.equal(out4, out4_ref)
+    rgb = torch.empty(B, 3, device="cuda")
+    N.call("dv_composite_fwd", B, N.ptr(seg.offsets), N.ptr(out4), 1, N.ptr(rgb), None, None, st)
+    g_rgb = (torch.rand(B, 3, generator=torch.Generator().manual_seed(3)) - 0.5).cuda()
+    d4 = torch.empty_like(out4)
+    N.call("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb), 1e-5 / B, None,
+           N.ptr(d4), st)
+    grads = []
+    for sv in (save, None):
+        gv = torch.zeros_like(field.voxels)
+        gp = torch.zeros_like(field.params)
+        assert tw.backward(k, field.voxels, seg, pe_feat, pe_out, d4, gv, gp, st, sv, out4)
+        torch.cuda.synchronize()
+        assert int(tw.err.item()) == 0
+        grads.append((gv, gp))
+    for a, b in zip(*grads):
+        assert (a - b).abs().max().item() <= 1e-6 * a.abs().max().item()
