@@ -32,17 +32,37 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mrays/s render & train fwd+bwd, p50/p99 frame ms; fused BF16 vs plain FP32 @ tol"
 BATCH = 4096
 L_S = 1e-5
-# Algorithmic FLOPs per segment (2 x multiply-adds), DIVeR32 with 32 channels:
-#   decoder forward  4224 MACs (mlp1 3 layers, mlp2 hidden part + output; the PE
-#                    part of mlp2's first layer is per ray) + 256 (integral)
-#   decoder backward 4224 (input grads) + 5088 (weight grads incl. PE rows)
-#                    + 256 (integral) + 256 (corner scatter) + 4224 (recompute)
-FLOP_PER_SEG = {"dv_decode_fwd": 2 * (4224 + 256), "dv_decode_bwd": 2 * (4224 + 5088 + 256 + 256 + 4224 + 256)}
-# DRAM bytes per launch of the dominant kernel (dram__bytes_read.sum + dram__bytes_write.sum,
-# one ncu capture of a training step of this workload, ~1.0 M segments; profiles/)
-TRAFFIC_PER_LAUNCH = {"dv_decode_bwd": 1157349888 + 505501184}
-FLOP_PER_SEG["dv_decode_bwd_tc"] = FLOP_PER_SEG["dv_decode_bwd"]
-FLOP_PER_SEG["dv_decode_fwd_tc"] = FLOP_PER_SEG["dv_decode_fwd"]
+# Algorithmic work of the decode kernels (the roofline's numerator), DIVeR32 over
+# 32 channels, per launch of S segments of R rays touching U distinct corner rows:
+#   FLOPs   forward 10,176 per segment (2 x multiply-adds of the torch-form decoder
+#           incl. the per-segment PE part), backward 2 x that (input + weight grads)
+#   bytes   compulsory HBM bytes: corner rows U x 128 B (read by a forward,
+#           read-modify-written once by a backward's gradient accumulation), the
+#           segment record + ray id (28 B), out4 / d4 (16 B each), the per-ray PE
+#           rows (pe_feat 112 B, pe_out 128 B), and the 320 B of BF16 layer tiles per
+#           segment that the tensor-core forward saves and its backward reads back
+ROW_BYTES = 32 * 4
+FLOP_FWD_SEG = 10176
+
+
+def alg_work(kernel, S, U, R):
+    """(FLOPs, bytes) of one launch."""
+    if kernel == "dv_decode_bwd_tc":
+        return 2 * FLOP_FWD_SEG * S, 2 * U * ROW_BYTES + S * (28 + 16 + 16 + 320) + R * (112 + 128)
+    if kernel == "dv_decode_bwd":
+        return 2 * FLOP_FWD_SEG * S, 3 * U * ROW_BYTES + S * (28 + 16) + R * (112 + 128)
+    if kernel == "dv_decode_fwd_tc":
+        return FLOP_FWD_SEG * S, U * ROW_BYTES + S * (28 + 16 + 320) + R * 128
+    if kernel == "dv_decode_fwd":
+        return FLOP_FWD_SEG * S, U * ROW_BYTES + S * (28 + 16) + R * 128
+    return 0, 0
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per segment of the
+# dominant kernels, from one ncu capture of the captured training step of this
+# workload (profiles/decode_bwd_tc_train.md); the roofline's `traffic` is this
+# times the segments of a launch.
+TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52}
 OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd(_tc), composite_fwd, composite_bwd,
 #                             decode_bwd(_tc)
 
@@ -175,6 +195,23 @@ def make_batches(scene, count, device, seed=4):
     return scenes.training_batches(scene, count, BATCH, device, seed)
 
 
+def unique_corner_rows(seg, n):
+    """Distinct grid rows (corner vertices) that the segments' integrals read,
+    on a cubic grid of n vertices per side (the corner rule of the decode kernels)."""
+    import torch
+
+    lo = torch.minimum((seg.seg[:, :3] + 1e-4).long(), (seg.seg[:, 3:] + 1e-4).long()).clamp_(0, n - 1)
+    rows = []
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                x = (lo[:, 0] + dx).clamp_max(n - 1)
+                y = (lo[:, 1] + dy).clamp_max(n - 1)
+                z = (lo[:, 2] + dz).clamp_max(n - 1)
+                rows.append((z * n + y) * n + x)
+    return int(torch.unique(torch.cat(rows)).numel())
+
+
 def train_step(field, o, d, tgt, form="fp32"):
     import torch
 
@@ -248,7 +285,12 @@ def run_ours(args, rank, world, local):
     ms, clocks = graphs[tform]
     kernel_ms = forms[tform][1]
     # segments per step (for the roofline): recount with the same traversal
-    seg_counts = [field.segments(*batches[args.warmup + i][:2]).total for i in range(args.steps)]
+    seg_counts, corner_rows = [], []
+    for i in range(args.steps):
+        seg = field.segments(*batches[args.warmup + i][:2])
+        seg_counts.append(seg.total)
+        corner_rows.append(unique_corner_rows(seg, field.voxels.shape[0]))
+        del seg
     ms_max = allreduce_max(ms, world)
     rays = allreduce_sum(float(BATCH * args.steps), world)
     value = rays / (ms_max * 1e-3) / 1e6
@@ -316,14 +358,27 @@ def run_ours(args, rank, world, local):
     tot = {k: sum(v) for k, v in kernel_ms.items()}
     dom = max(tot, key=tot.get)
     avg_ms = tot[dom] / len(kernel_ms[dom])
-    flops = FLOP_PER_SEG.get(dom, 0) * statistics.mean(seg_counts)
-    peak = peaks.get("bf16_tflops_sustained", 1700.0)
-    achieved = flops / (avg_ms * 1e-3) / 1e12 if flops else None
-    roofline = {"kernel": dom, "bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": (achieved / peak) if achieved else None, "traffic": TRAFFIC_PER_LAUNCH.get(dom),
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (measured)" if peaks else "fallback",
-                "avg_launch_ms": avg_ms, "segments_per_launch": statistics.mean(seg_counts),
-                "kernel_share": {k: v / sum(tot.values()) for k, v in tot.items()}}
+    S_mean = statistics.mean(seg_counts)
+    U_mean = statistics.mean(corner_rows)
+    flops, nbytes = alg_work(dom, S_mean, U_mean, BATCH)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    tensor = peaks.get("bf16_tflops_sustained", 1700.0)
+    t_bytes, t_flops = nbytes / (hbm * 1e9), flops / (tensor * 1e12)
+    sec = avg_ms * 1e-3
+    if t_bytes >= t_flops:
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": nbytes / sec / 1e9, "peak": hbm, "unit": "GB/s",
+                    "frac": nbytes / sec / 1e9 / hbm,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback"}
+    else:
+        roofline = {"kernel": dom, "bound": "tensor", "achieved": flops / sec / 1e12, "peak": tensor,
+                    "unit": "TFLOP/s", "frac": flops / sec / 1e12 / tensor,
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (measured)" if peaks else "fallback"}
+    roofline.update({
+        "traffic": TRAFFIC_PER_SEG[dom] * S_mean if dom in TRAFFIC_PER_SEG else None,
+        "algorithmic_bytes": nbytes, "algorithmic_flops": flops,
+        "tensor_frac": flops / sec / 1e12 / tensor, "hbm_frac": nbytes / sec / 1e9 / hbm,
+        "avg_launch_ms": avg_ms, "segments_per_launch": S_mean, "corner_rows_per_launch": U_mean,
+        "kernel_share": {k: v / sum(tot.values()) for k, v in tot.items()}})
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -4,7 +4,10 @@ of 4096 rays that hit occupied voxels, one step captured in a CUDA graph
 cudaProfilerStart/Stop are the ones a profiler started with
 --profile-from-start off records; the timed replays after them are printed.
 
-    python -m diver_gb300.profile_train --form bf16 --profiled 3 --timed 20
+    python -m diver_gb300.profile_train --form bf16 --profiled 3 --timed 20 [--grid 128]
+
+--grid selects a smaller n^3 x 32 grid of the same scene family (for profiler
+captures that replay kernels many times).
 """
 from __future__ import annotations
 
@@ -23,12 +26,15 @@ def main():
     p.add_argument("--batch", type=int, default=4096)
     p.add_argument("--profiled", type=int, default=3)
     p.add_argument("--timed", type=int, default=20)
+    p.add_argument("--grid", type=int, default=256)
     args = p.parse_args()
     dev = torch.device("cuda")
-    sc = scenes.grid_scene(256, 32, "diver32", device=dev)
+    sc = scenes.grid_scene(args.grid, 32, "diver32", device=dev)
     field = DIVeRField.from_scene(sc, dev)
     batches = scenes.training_batches(sc, 6, args.batch, dev)
     step = TrainStepGraph(field, *batches[0], form=args.form)
+    counts = [field.segments(*batches[1 + i % 5][:2]).total for i in range(args.profiled)]
+    print(f"segments of the profiled steps: {counts} (total {sum(counts)})", flush=True)
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()
     for i in range(args.profiled):
@@ -41,7 +47,8 @@ def main():
         step(*batches[i % 6])
     e1.record()
     torch.cuda.synchronize()
-    print(f"{args.form} captured step: {e0.elapsed_time(e1) / args.timed:.3f} ms (batch {args.batch})", flush=True)
+    print(f"{args.form} captured step: {e0.elapsed_time(e1) / args.timed:.3f} ms (batch {args.batch}, "
+          f"grid {args.grid}^3)", flush=True)
 
 
 if __name__ == "__main__":
