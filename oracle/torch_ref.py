@@ -20,9 +20,12 @@ import math
 import torch
 
 
-def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor, per_axis: bool = False) -> torch.Tensor:
+def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor, per_axis: bool = False,
+              dtype: torch.dtype | None = None) -> torch.Tensor:
     """per_axis: clamp each axis to its own vertex count (grids that are not
-    cubic); the reference clamps every axis with voxels.shape[-2]."""
+    cubic); the reference clamps every axis with voxels.shape[-2].  dtype:
+    arithmetic type when it differs from the grid's (the corner rows are
+    gathered first, then converted, so a large FP32 grid needs no FP64 copy)."""
     n, c = voxels.shape[-2:]
     pmin = torch.min((coord_i + 1e-4).long(), (coord_o + 1e-4).long())
     xmin, ymin, zmin = pmin.split(1, dim=-1)
@@ -34,8 +37,9 @@ def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor
         xmax, ymax, zmax = (pmin + 1).clamp_max(n - 1).split(1, dim=-1)
     corners = [voxels[zmin, ymin, xmin], voxels[zmin, ymin, xmax], voxels[zmin, ymax, xmin], voxels[zmin, ymax, xmax],
                voxels[zmax, ymin, xmin], voxels[zmax, ymin, xmax], voxels[zmax, ymax, xmin], voxels[zmax, ymax, xmax]]
-    F = torch.stack(corners, 0).reshape(2, 2, 2, -1, c)  # [z][y][x]
-    P = torch.stack([coord_i - pmin, coord_o - pmin], 0).permute(0, 2, 1).to(voxels.dtype)  # [2][xyz][S]
+    dt = dtype or voxels.dtype
+    F = torch.stack(corners, 0).reshape(2, 2, 2, -1, c).to(dt)  # [z][y][x]
+    P = torch.stack([coord_i - pmin, coord_o - pmin], 0).permute(0, 2, 1).to(dt)  # [2][xyz][S]
     A = P.sum(0).prod(0) / 12 + P.prod(1).sum(0) / 6
     X = F[1] - F[0]
     X = X[0] - X[1]
@@ -98,9 +102,9 @@ def render(color: torch.Tensor, sigma: torch.Tensor, mask: torch.Tensor, white_b
     return rgb, weight
 
 
-def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True, per_axis=False):
+def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True, per_axis=False, dtype=None):
     """Full decode path over CSR segments: returns rgb [B,3], sigma [B,M], mask [B,M]."""
-    feat = integrate(voxels, seg[:, :3], seg[:, 3:], per_axis)
+    feat = integrate(voxels, seg[:, :3], seg[:, 3:], per_axis, dtype)
     s, c = decode(layers, n_mlp1, feat, dirs[seg_ray.long()])
     sigma, mask = scatter_padded(s, counts)
     color, _ = scatter_padded(c, counts)
