@@ -501,12 +501,18 @@ def run_realtime(args, dev):
         frames.append((cams[k][:, 3], d))
     rounds = []
 
-    def frame(i):
-        _, r = model.render_frame(*frames[i % 3])
+    def frame_loop(i):
+        _, r = model.render_frame(*frames[i % 3], fused=False)
         rounds.append(r)
 
-    ms = _time_steps(frame, 1, 3)
-    return {"frame_ms": ms, "Mrays_per_s": 640000 / (ms * 1e-3) / 1e6, "rounds": rounds[-1],
+    def frame_fused(i):
+        model.render_frame(*frames[i % 3])
+
+    ms_loop = _time_steps(frame_loop, 1, 3)
+    ms = _time_steps(frame_fused, 3, 10)
+    return {"frame_ms": ms, "Mrays_per_s": 640000 / (ms * 1e-3) / 1e6, "form": "one launch per frame",
+            "host_loop": {"frame_ms": ms_loop, "rounds": rounds[-1],
+                          "form": "aabb_intersect + rounds of ray_march / mlp_eval (the reference's loop)"},
             "features": int(ser["f"].shape[0])}
 
 

@@ -99,15 +99,90 @@ struct RtArgs {
 
 __device__ __forceinline__ int clampi(int x, int hi) { return x < 0 ? 0 : (x > hi ? hi : x); }
 
+// One recorded hit (segment p0 -> p1 in fine voxel units) of one pixel:
+// integral of the sparse feature table, the folded MLP, and front-to-back
+// compositing into acc (rgb, T).  Returns false when the pixel is finished
+// (T < 1e-2).  Shared by the per-round kernel and the fused frame kernel so
+// both perform the same arithmetic.
+template <int W, int FIRST>
+__device__ __forceinline__ bool rt_eval_hit(const float* __restrict__ sw, float* X, float* H, const float* pe,
+                                            const float* __restrict__ feats, const int* __restrict__ vmap, int ms,
+                                            float x0, float y0, float z0, float x1, float y1, float z1,
+                                            float4& acc) {
+  using L = RtLayout<W, FIRST>;
+  float y[W + 4];
+  // corner weights; the index clamp of segment_corners is replaced by the
+  // texture-style clamp of each lookup (mlp_eval.cu:112-118)
+  const SegCorner sc = segment_corners(x0, y0, z0, x1, y1, z1, 1 << 30, 1 << 30, 1 << 30);
+  float f[32];
+#pragma unroll
+  for (int k = 0; k < 32; ++k) f[k] = FIRST ? sw[L::b_in + k] : 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int x = clampi(sc.x + (j & 1), ms - 1);
+    const int yy = clampi(sc.y + ((j >> 1) & 1), ms - 1);
+    const int z = clampi(sc.z + (j >> 2), ms - 1);
+    const int idx = __ldg(vmap + ((long long)z * ms + yy) * ms + x);
+    const float4* row = reinterpret_cast<const float4*>(feats + (long long)idx * 32);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 v = __ldg(row + q);
+      f[4 * q] = fmaf(sc.w[j], v.x, f[4 * q]);
+      f[4 * q + 1] = fmaf(sc.w[j], v.y, f[4 * q + 1]);
+      f[4 * q + 2] = fmaf(sc.w[j], v.z, f[4 * q + 2]);
+      f[4 * q + 3] = fmaf(sc.w[j], v.w, f[4 * q + 3]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 32; ++k) X[k] = FIRST ? fmaxf(f[k], 0.f) : f[k];
+  dense_fwd_s<W, false>(sw + L::l0_w, sw + L::l0_b, X, 32, y);
+#pragma unroll
+  for (int k = 0; k < W; ++k) H[k] = fmaxf(y[k], 0.f);
+  float sigma = sw[L::sig + W];
+#pragma unroll 8
+  for (int k = 0; k < W; ++k) sigma = fmaf(sw[L::sig + k], H[k], sigma);
+  const float alpha = 1.f - expf(-fmaxf(sigma, 0.f));
+  if (alpha < 1e-2f) return true;
+  dense_fwd_s<W, false>(sw + L::l2_w, sw + L::l2_b, H, W, y);
+#pragma unroll
+  for (int k = 0; k < PE_DIM; ++k) {
+    const float p = pe[k];
+#pragma unroll
+    for (int j = 0; j < W; j += 4) {
+      const float4 w = *reinterpret_cast<const float4*>(sw + L::l2_pe + k * W + j);
+      y[j] = fmaf(p, w.x, y[j]);
+      y[j + 1] = fmaf(p, w.y, y[j + 1]);
+      y[j + 2] = fmaf(p, w.z, y[j + 2]);
+      y[j + 3] = fmaf(p, w.w, y[j + 3]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < W; ++k) X[k] = fmaxf(y[k], 0.f);
+  float o[4];
+  dense_fwd_s<4, false>(sw + L::l3_w, sw + L::l3_b, X, W, o);
+  const float wgt = acc.w * alpha;
+  acc.x += wgt * sigmoidf_acc(o[0]);
+  acc.y += wgt * sigmoidf_acc(o[1]);
+  acc.z += wgt * sigmoidf_acc(o[2]);
+  acc.w = acc.w * (1.f - alpha);
+  return !(acc.w < 1e-2f);
+}
+
+template <int W, int FIRST>
+__device__ __forceinline__ void stage_weights(const float* __restrict__ params, float* sw) {
+  using L = RtLayout<W, FIRST>;
+  for (int i = threadIdx.x; i < L::size / 4; i += blockDim.x)
+    reinterpret_cast<float4*>(sw)[i] = __ldg(reinterpret_cast<const float4*>(params) + i);
+  __syncthreads();
+}
+
 template <int W, int FIRST>
 __global__ void __launch_bounds__(128) mlp_eval_kernel(const RtArgs a) {
   using L = RtLayout<W, FIRST>;
   extern __shared__ __align__(16) float smem[];
   float* sw = smem;
   float* rows = smem + L::size;
-  for (int i = threadIdx.x; i < L::size / 4; i += blockDim.x)
-    reinterpret_cast<float4*>(sw)[i] = __ldg(reinterpret_cast<const float4*>(a.params) + i);
-  __syncthreads();
+  stage_weights<W, FIRST>(a.params, sw);
   float* X = rows + threadIdx.x * (W + 4);               // integrated feature / h2
   float* H = rows + (blockDim.x + threadIdx.x) * (W + 4);  // h1
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,72 +191,130 @@ __global__ void __launch_bounds__(128) mlp_eval_kernel(const RtArgs a) {
   pos_enc(__ldg(a.v + 3 * b), __ldg(a.v + 3 * b + 1), __ldg(a.v + 3 * b + 2), pe);
   float4 acc = reinterpret_cast<float4*>(a.rgba)[b];
   const long long stride = (long long)a.batch * 6;
-  float y[W + 4];
   for (int hit = 0; hit < 8; ++hit) {
     const float* c = a.coords + hit * stride + (long long)b * 6;
-    const float x0 = c[0], y0 = c[1], z0 = c[2], x1 = c[3], y1 = c[4], z1 = c[5];
-    if (x0 < 0.f) {
+    if (c[0] < 0.f) {
       a.finish[b] = 1;
       break;
     }
-    // corner weights; the index clamp of segment_corners is replaced by the
-    // texture-style clamp of each lookup (mlp_eval.cu:112-118)
-    const SegCorner sc = segment_corners(x0, y0, z0, x1, y1, z1, 1 << 30, 1 << 30, 1 << 30);
-    float f[32];
-#pragma unroll
-    for (int k = 0; k < 32; ++k) f[k] = FIRST ? sw[L::b_in + k] : 0.f;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int x = clampi(sc.x + (j & 1), a.ms - 1);
-      const int yy = clampi(sc.y + ((j >> 1) & 1), a.ms - 1);
-      const int z = clampi(sc.z + (j >> 2), a.ms - 1);
-      const int idx = __ldg(a.vmap + ((long long)z * a.ms + yy) * a.ms + x);
-      const float4* row = reinterpret_cast<const float4*>(a.feats + (long long)idx * 32);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 v = __ldg(row + q);
-        f[4 * q] = fmaf(sc.w[j], v.x, f[4 * q]);
-        f[4 * q + 1] = fmaf(sc.w[j], v.y, f[4 * q + 1]);
-        f[4 * q + 2] = fmaf(sc.w[j], v.z, f[4 * q + 2]);
-        f[4 * q + 3] = fmaf(sc.w[j], v.w, f[4 * q + 3]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < 32; ++k) X[k] = FIRST ? fmaxf(f[k], 0.f) : f[k];
-    dense_fwd_s<W, false>(sw + L::l0_w, sw + L::l0_b, X, 32, y);
-#pragma unroll
-    for (int k = 0; k < W; ++k) H[k] = fmaxf(y[k], 0.f);
-    float sigma = sw[L::sig + W];
-#pragma unroll 8
-    for (int k = 0; k < W; ++k) sigma = fmaf(sw[L::sig + k], H[k], sigma);
-    const float alpha = 1.f - expf(-fmaxf(sigma, 0.f));
-    if (alpha < 1e-2f) continue;
-    dense_fwd_s<W, false>(sw + L::l2_w, sw + L::l2_b, H, W, y);
-#pragma unroll
-    for (int k = 0; k < PE_DIM; ++k) {
-      const float p = pe[k];
-#pragma unroll
-      for (int j = 0; j < W; j += 4) {
-        const float4 w = *reinterpret_cast<const float4*>(sw + L::l2_pe + k * W + j);
-        y[j] = fmaf(p, w.x, y[j]);
-        y[j + 1] = fmaf(p, w.y, y[j + 1]);
-        y[j + 2] = fmaf(p, w.z, y[j + 2]);
-        y[j + 3] = fmaf(p, w.w, y[j + 3]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < W; ++k) X[k] = fmaxf(y[k], 0.f);
-    float o[4];
-    dense_fwd_s<4, false>(sw + L::l3_w, sw + L::l3_b, X, W, o);
-    const float wgt = acc.w * alpha;
-    acc.x += wgt * sigmoidf_acc(o[0]);
-    acc.y += wgt * sigmoidf_acc(o[1]);
-    acc.z += wgt * sigmoidf_acc(o[2]);
-    acc.w = acc.w * (1.f - alpha);
-    if (acc.w < 1e-2f) {
+    if (!rt_eval_hit<W, FIRST>(sw, X, H, pe, a.feats, a.vmap, a.ms, c[0], c[1], c[2], c[3], c[4], c[5], acc)) {
       a.finish[b] = 1;
       break;
     }
+  }
+  reinterpret_cast<float4*>(a.rgba)[b] = acc;
+}
+
+// Whole frame in one launch: per pixel, the octree first hit, then rounds of
+// (walk the fine occupancy mask to the next 8 occupied voxels, decode them)
+// until the ray leaves the grid or T < 1e-2.  The per-ray arithmetic and its
+// order are those of the host loop aabb_intersect + rounds of (ray_march,
+// mlp_eval) (eval_rt.py:115-122); the rounds simply continue inside the
+// kernel, with the hits in shared memory instead of a coords buffer and no
+// host round trip between them.
+struct RtFrameArgs {
+  int batch;
+  const float* v;        // [B][3] unit directions
+  const float* center;   // [3] camera centre, fine voxel units (device)
+  const uint8_t* oct;    // octree levels (scales 64, 16, 4), coarsest first
+  long long oct_cells;
+  const uint8_t* mask;   // [N][N][N] fine occupancy
+  int N;
+  const float* feats;
+  const int* vmap;
+  int ms;
+  const float* params;
+  float* rgba;           // [B][4] (rgb, T)
+};
+
+template <int W, int FIRST, bool FAST>
+__device__ __forceinline__ void rt_frame_ray(const RtFrameArgs& a, const float* sw, float* X, float* H,
+                                             float* hit_slots, int b, float3 p, const float3 d, float4& acc) {
+  const float3 s = make_float3(step_sign(d.x), step_sign(d.y), step_sign(d.z));
+  const float3 r = FAST ? make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z)) : d;
+  // octree: level 0 cells of 64^3 voxels, descend x4 on an occupied cell
+  int m = a.N / 64;
+  long long off = 0;
+  float3 last = p;
+  while (m < a.N) {
+    last = p;
+    float3 q;
+    float dt;
+    grid_step<FAST>(last, d, r, s, q, dt);
+    if (outside_closed(q, (float)m)) return;
+    if (occupied(a.oct, off + cell_index1(last, q, m), a.oct_cells)) {
+      off += (long long)m * m * m;
+      last = make_float3(__fmul_rn(last.x, 4.f), __fmul_rn(last.y, 4.f), __fmul_rn(last.z, 4.f));
+      p = last;
+      m *= 4;
+    } else {
+      p = q;
+    }
+  }
+  float pe[PE_PAD];
+  pos_enc(d.x, d.y, d.z, pe);
+  const float n = (float)a.N;
+  const long long cells = (long long)a.N * a.N * a.N;
+  // Rounds as in the host loop: march to the next 8 occupied voxels (kept in
+  // this thread's shared-memory slots), then decode them.  Keeping the walk
+  // and the decode in separate phases keeps a warp's lanes in the same phase;
+  // decoding each hit as it is found would make every DDA step wait for the
+  // lanes that decode.
+  float* hits = hit_slots;  // [8][6] per thread
+  while (true) {
+    int nh = 0;
+    bool out = false;
+    while (nh < 8) {
+      float3 q;
+      float dt;
+      grid_step<FAST>(last, d, r, s, q, dt);
+      if (outside_open(q, n)) {
+        out = true;
+        break;
+      }
+      if (occupied(a.mask, cell_index1(last, q, a.N), cells)) {
+        float* h = hits + nh * 6;
+        h[0] = last.x;
+        h[1] = last.y;
+        h[2] = last.z;
+        h[3] = q.x;
+        h[4] = q.y;
+        h[5] = q.z;
+        ++nh;
+      }
+      last = q;
+    }
+    for (int k = 0; k < nh; ++k) {
+      const float* h = hits + k * 6;
+      if (!rt_eval_hit<W, FIRST>(sw, X, H, pe, a.feats, a.vmap, a.ms, h[0], h[1], h[2], h[3], h[4], h[5], acc))
+        return;
+    }
+    if (out) return;
+  }
+}
+
+template <int W, int FIRST>
+__global__ void __launch_bounds__(128) rt_frame_kernel(const RtFrameArgs a) {
+  using L = RtLayout<W, FIRST>;
+  extern __shared__ __align__(16) float smem[];
+  float* sw = smem;
+  float* rows = smem + L::size;
+  stage_weights<W, FIRST>(a.params, sw);
+  float* X = rows + threadIdx.x * (W + 4);
+  float* H = rows + (blockDim.x + threadIdx.x) * (W + 4);
+  float* hit_slots = rows + 2 * blockDim.x * (W + 4) + threadIdx.x * 48;
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.batch) return;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 1.f);
+  const float3 d = make_float3(__ldg(a.v + 3 * b), __ldg(a.v + 3 * b + 1), __ldg(a.v + 3 * b + 2));
+  float3 p = make_float3(__ldg(a.center), __ldg(a.center + 1), __ldg(a.center + 2));
+  float t;
+  if (box_entry(p, d, (float)a.N, t)) {
+    p = make_float3(__fmul_rn(p.x, 0.015625f), __fmul_rn(p.y, 0.015625f), __fmul_rn(p.z, 0.015625f));
+    if (a.N < (1 << 22) && recip_ok(d))
+      rt_frame_ray<W, FIRST, true>(a, sw, X, H, hit_slots, b, p, d, acc);
+    else
+      rt_frame_ray<W, FIRST, false>(a, sw, X, H, hit_slots, b, p, d, acc);
   }
   reinterpret_cast<float4*>(a.rgba)[b] = acc;
 }
@@ -191,6 +324,17 @@ int launch_mlp_eval(const RtArgs& a, cudaStream_t st) {
   using L = RtLayout<W, FIRST>;
   const size_t smem = (size_t)(L::size + 2 * 128 * (W + 4)) * sizeof(float);
   auto k = mlp_eval_kernel<W, FIRST>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
+  k<<<ceil_div(a.batch, 128), 128, smem, st>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+template <int W, int FIRST>
+int launch_rt_frame(const RtFrameArgs& a, cudaStream_t st) {
+  using L = RtLayout<W, FIRST>;
+  const size_t smem = (size_t)(L::size + 2 * 128 * (W + 4) + 128 * 48) * sizeof(float);
+  auto k = rt_frame_kernel<W, FIRST>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
   k<<<ceil_div(a.batch, 128), 128, smem, st>>>(a);
   DV_TRY_LAUNCH();
@@ -231,6 +375,21 @@ int dv_mlp_eval(int width, int batch_size, const float* coords, const float* vox
   RtArgs a{batch_size, coords, voxels, voxel_map, map_size, packed_params, v, rgba, finish};
   cudaStream_t st = (cudaStream_t)stream;
   return width == 32 ? launch_mlp_eval<32, 1>(a, st) : launch_mlp_eval<64, 0>(a, st);
+}
+
+int dv_realtime_frame(int width, int batch_size, const float* v, const float* center, const uint8_t* octrees, int N,
+                      const uint8_t* voxel_mask, const float* voxels, const int* voxel_map, int map_size,
+                      const float* packed_params, float* rgba, void* stream) {
+  DV_CHECK((width == 32 || width == 64) && batch_size >= 0 && N > 0 && N % 64 == 0 && map_size == N + 1, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(v && center && octrees && voxel_mask && voxels && voxel_map && packed_params && rgba, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)voxels & 15) == 0 && ((uintptr_t)rgba & 15) == 0 && ((uintptr_t)packed_params & 15) == 0,
+           DV_ERR_ARG);
+  const long long n64 = N / 64, n16 = N / 16, n4 = N / 4;
+  RtFrameArgs a{batch_size, v, center, octrees, n64 * n64 * n64 + n16 * n16 * n16 + n4 * n4 * n4, voxel_mask, N,
+                voxels, voxel_map, map_size, packed_params, rgba};
+  cudaStream_t st = (cudaStream_t)stream;
+  return width == 32 ? launch_rt_frame<32, 1>(a, st) : launch_rt_frame<64, 0>(a, st);
 }
 
 }  // extern "C"

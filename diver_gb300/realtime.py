@@ -92,14 +92,26 @@ class RealtimeModel:
         N.call("dv_mlp_eval", self.width, B, N.ptr(coords), N.ptr(self.features), N.ptr(self.voxel_map),
                self.voxel_map.shape[0], N.ptr(self.packed), N.ptr(v), N.ptr(rgba), N.ptr(fin), N.stream(v.device))
 
-    def render_frame(self, eye: torch.Tensor, dirs: torch.Tensor, max_rounds: int | None = None):
+    def render_frame(self, eye: torch.Tensor, dirs: torch.Tensor, max_rounds: int | None = None,
+                     fused: bool = True):
         """rgb [B,3] of B rays from camera centre `eye` (world) with unit
         directions `dirs` [B,3] (eval_rt.py:106-122); also returns the number of
-        march/decode rounds."""
+        host rounds.  fused (default): the whole frame in one launch
+        (dv_realtime_frame, same result); otherwise the reference's loop of
+        aabb_intersect, then ray_march + mlp_eval rounds until every pixel is
+        finished (max_rounds caps it)."""
         dev = dirs.device
         B = dirs.shape[0]
         v = dirs.contiguous()
         center = ((eye.float().cpu() - self.xyzmin) / self.voxel_size).to(dev).contiguous()
+        if fused:
+            rgba = torch.empty(B, 4, device=dev)
+            m8 = self.voxel_masks.view(torch.uint8) if self.voxel_masks.dtype == torch.bool else self.voxel_masks
+            o8 = self.octrees.view(torch.uint8) if self.octrees.dtype == torch.bool else self.octrees
+            N.call("dv_realtime_frame", self.width, B, N.ptr(v), N.ptr(center), N.ptr(o8), self.voxel_num, N.ptr(m8),
+                   N.ptr(self.features), N.ptr(self.voxel_map), self.voxel_map.shape[0], N.ptr(self.packed),
+                   N.ptr(rgba), N.stream(dev))
+            return rgba[:, :3] + rgba[:, 3:], 1
         coords = torch.zeros(8, B, 6, device=dev)
         rgba = torch.zeros(B, 4, device=dev)
         finish = torch.zeros(B, dtype=torch.bool, device=dev)

@@ -350,6 +350,22 @@ DV_API int dv_mlp_eval(int width, int batch_size, const float* coords, const flo
                        const int* voxel_map, int map_size, const float* packed_params, const float* v,
                        float* rgba, uint8_t* finish, void* stream);
 
+/*
+ * Whole real-time frame in one launch (no counterpart call in the reference,
+ * whose eval_rt.py:115-122 loops on the host: dv_aabb_intersect, then rounds
+ * of dv_ray_march + dv_mlp_eval until every pixel is finished).  Per pixel:
+ * the octree first hit, then the fine-grid walk, each occupied voxel decoded
+ * as it is reached, until the ray leaves the grid or T < 1e-2.  Same per-pixel
+ * arithmetic and order as the host loop, so rgba [batch][4] (rgb, T) equals
+ * its result; center is the camera centre in voxel units (device [3]);
+ * octrees / voxel_mask / voxels / voxel_map / packed_params as for
+ * dv_aabb_intersect, dv_ray_march and dv_mlp_eval (map_size = N + 1).
+ */
+DV_API int dv_realtime_frame(int width, int batch_size, const float* v, const float* center,
+                             const uint8_t* octrees, int N, const uint8_t* voxel_mask,
+                             const float* voxels, const int* voxel_map, int map_size,
+                             const float* packed_params, float* rgba, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

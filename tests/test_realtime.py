@@ -69,7 +69,10 @@ def test_realtime_frame_matches_oracle_loop(kind, width):
     sc, ser, model = small_realtime(kind, "cuda")
     c2w = scenes.sphere_cameras(1, 4.0, 3)[0]
     o, v = scenes.camera_rays(c2w, 128, 128, 153.6, "cpu")
-    rgb, rounds = model.render_frame(c2w[:, 3], v.cuda())
+    rgb, rounds = model.render_frame(c2w[:, 3], v.cuda(), fused=False)
+    rgb_fused, _ = model.render_frame(c2w[:, 3], v.cuda())
+    # the single-launch frame performs the same per-pixel arithmetic as the loop
+    assert torch.equal(rgb_fused, rgb)
     # oracle: same loop with the C restatements
     B = v.shape[0]
     center = ((c2w[:, 3].float() - sc.xyzmin) / sc.voxel_size).numpy().astype(np.float32)
