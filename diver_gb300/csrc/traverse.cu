@@ -200,9 +200,7 @@ struct SegWriter {
 // their occupancy loads back to back, then records the occupied ones in
 // order, so a ray waits for one load latency per LOOKAHEAD voxels instead of
 // one per voxel (which bounds small batches, where few warps are resident).
-constexpr int LOOKAHEAD = 8;
-
-template <int MODE, bool FAST>
+template <int MODE, bool FAST, int LOOKAHEAD>
 __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, const float3 d, float t) {
   const float3 s = signs(d);
   const float3 r = FAST ? recip3(d) : d;
@@ -271,8 +269,11 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
   return count;
 }
 
+// 16 steps ahead when counting (few registers per step), 8 when the segments
+// are also written.
 template <int MODE>
 __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
+  constexpr int K = MODE == WALK_COUNT ? 16 : 8;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = b < a.batch;
   int count = 0;
@@ -281,7 +282,8 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
     float3 p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
     float t;
     if (box_entry3(p, d, a.n3, t))
-      count = (a.fast && recip_ok(d)) ? masked_walk<MODE, true>(a, b, p, d, t) : masked_walk<MODE, false>(a, b, p, d, t);
+      count = (a.fast && recip_ok(d)) ? masked_walk<MODE, true, K>(a, b, p, d, t)
+                                      : masked_walk<MODE, false, K>(a, b, p, d, t);
     if (MODE != WALK_SEGMENTS) a.num[b] = count;
   }
   if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
@@ -493,6 +495,27 @@ static int cells_per_side(float n, float scale) {
   return (int)prod;
 }
 
+// Threads per block of a walk launch.  One thread walks one ray and the walk
+// is a long dependent chain, so a small batch runs faster spread thinly: with
+// fewer rays than 8 warps per SM, blocks of one warp put each warp on its own
+// SM instead of several warps sharing a scheduler.
+static int walk_block(int batch) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return batch < sms * 256 ? 32 : 256;
+}
+
+#define DV_WALK_LAUNCH(kernel, batch, stream, args)                              \
+  do {                                                                             \
+    const int bs__ = walk_block(batch);                                            \
+    kernel<<<ceil_div((batch), bs__), bs__, 0, (cudaStream_t)(stream)>>>(args);   \
+  } while (0)
+
 static bool aligned_to(const void* p, uintptr_t n) { return ((uintptr_t)p % n) == 0; }
 
 // The segment writers store seg with 16-byte (masked) or 8-byte (dense)
@@ -536,7 +559,7 @@ int dv_ray_voxel_intersect(int batch_size, int max_n, float xyzmin, float xyzmax
   a.num = intersect_num;
   a.tns = tns;
   a.max_count = max_count;
-  dense_walk_kernel<WALK_PADDED><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(dense_walk_kernel<WALK_PADDED>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -550,7 +573,7 @@ int dv_ray_voxel_count(int batch_size, float xyzmin, float voxel_num, float voxe
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, 1.f, o, v, nullptr);
   a.num = intersect_num;
   a.max_count = max_count;
-  dense_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(dense_walk_kernel<WALK_COUNT>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -569,7 +592,7 @@ int dv_masked_intersect(int batch_size, int max_n, float xyzmin, float xyzmax, f
   a.num = intersect_num;
   a.tns = tns;
   a.max_count = max_count;
-  masked_walk_kernel<WALK_PADDED><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_PADDED>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -583,7 +606,7 @@ int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_s
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
-  masked_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_COUNT>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -601,7 +624,7 @@ int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxe
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
-  masked_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -618,7 +641,7 @@ int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, float voxel
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
-  dense_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(dense_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -660,7 +683,7 @@ int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, f
   WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
-  masked_walk_kernel<WALK_COUNT><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_COUNT>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -677,7 +700,7 @@ int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
-  masked_walk_kernel<WALK_SEGMENTS><<<ceil_div(batch_size, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

@@ -135,7 +135,7 @@ class TcWeights:
 class SegmentRender(Function):
     @staticmethod
     def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None,
-                voxels16: torch.Tensor | None = None):
+                voxels16: torch.Tensor | None = None, training: bool = False):
         nx, ny, nz, c = _grid(voxels)
         _check_params(kind, c, params)
         N.need_cuda("dirs", dirs, torch.float32)
@@ -153,7 +153,7 @@ class SegmentRender(Function):
                    S, seg.count_ptr, N.ptr(pe_out), N.ptr(out4), st)
         else:
             # training: keep the layer inputs for the tensor-core backward
-            save = tc.save_buffer(kind, c, S, dev) if (ctx.needs_input_grad[0] or ctx.needs_input_grad[1]) else None
+            save = tc.save_buffer(kind, c, S, dev) if training else None
             tc.decode(kind, c, voxels, seg, pe_out, out4, st, voxels16, save)
             ctx.saved_layers = save
         rgb = torch.empty(B, 3, device=dev)
@@ -191,10 +191,10 @@ class SegmentRender(Function):
         gp = torch.zeros_like(params)
         if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st,
                                                   getattr(ctx, "saved_layers", None), out4):
-            return gv, gp, None, None, None, None, None, None
+            return gv, gp, None, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
-        return gv, gp, None, None, None, None, None, None
+        return gv, gp, None, None, None, None, None, None, None
 
 
 def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None,
@@ -202,7 +202,11 @@ def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_b
     """(rgb [B,3], sparsity term) for the CSR segments of B rays.  `tc` selects
     the tensor-core decoder; `voxels16` (inference) is a BF16/FP16 copy of the
     grid the tensor-core forward reads its corner rows from."""
-    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16)
+    # whether a backward will follow is known here, not inside the Function's
+    # forward (which always runs with grad mode off): only then does the
+    # tensor-core forward keep its layer tiles for the backward
+    training = torch.is_grad_enabled() and (voxels.requires_grad or params.requires_grad)
+    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16, training)
 
 
 class DIVeRField(torch.nn.Module):

@@ -235,3 +235,20 @@ def test_render_error_metrics_vs_fp64(scene):
               f"max_abs_alpha={e_alpha:.3e} mean_alpha={ref_alpha.mean():.3f}")
         assert e_rgb <= ERR_BOUNDS[form], (form, e_rgb)
         assert e_alpha <= ERR_BOUNDS[form], (form, e_alpha)
+
+
+def test_inference_render_keeps_no_layer_tiles(monkeypatch):
+    """Without autograd the tensor-core forward must not keep its layer tiles
+    (for a 800x800 frame that buffer would be ~36 GB of writes)."""
+    from diver_gb300 import renderer
+
+    sc, o, v, field = small()
+
+    def refuse(*args, **kwargs):
+        raise AssertionError("layer-tile buffer requested by an inference render")
+
+    monkeypatch.setattr(renderer.TcWeights, "save_buffer", refuse)
+    with torch.no_grad():
+        rgb, _ = field(o.cuda(), v.cuda(), form="bf16")
+    torch.cuda.synchronize()
+    assert torch.isfinite(rgb).all()
