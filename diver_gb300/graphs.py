@@ -15,6 +15,8 @@ gradients, is recorded once in a CUDA graph and replayed.
 
 Inputs are copied into the graph's own buffers before each replay; outputs
 are the graph's buffers (overwritten by the next replay; clone to keep them).
+The grid gradient's zero fill (2.2 GB for a 256^3 x 32 grid) is issued on a
+second stream at the start of the step, and the backward waits for it.
 The tensor-core weight images are repacked from the parameters inside the
 graph, so optimizer steps between replays are seen by the next replay.
 """
@@ -47,6 +49,8 @@ class TrainStepGraph:
         self.field, self.form, self.l_s = field, form, float(l_s)
         self.o, self.d, self.target = o.clone().contiguous(), d.clone().contiguous(), target.clone().contiguous()
         self.capacity = field.segment_capacity(o.shape[0])
+        self._grid_grad = torch.zeros_like(field.voxels)
+        self._fill = torch.cuda.Stream(o.device)
         field.refresh_always = True
         try:
             self.graph, (self.loss, self.grad_voxels, self.grad_params) = _warm_and_capture(self._step, warmup)
@@ -55,7 +59,13 @@ class TrainStepGraph:
 
     def _step(self):
         f = self.field
-        rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity)
+        main = torch.cuda.current_stream()
+        self._fill.wait_stream(main)  # the previous step's use of the buffer is done
+        with torch.cuda.stream(self._fill):
+            self._grid_grad.zero_()
+            filled = torch.cuda.Event()
+            filled.record()
+        rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity, grad_voxels=(self._grid_grad, filled))
         loss = torch.nn.functional.mse_loss(rgb, self.target) + self.l_s * reg
         gv, gp = torch.autograd.grad(loss, [f.voxels, f.params])
         return loss.detach(), gv, gp

@@ -135,7 +135,7 @@ class TcWeights:
 class SegmentRender(Function):
     @staticmethod
     def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None,
-                voxels16: torch.Tensor | None = None, training: bool = False):
+                voxels16: torch.Tensor | None = None, training: bool = False, grad_voxels=None):
         nx, ny, nz, c = _grid(voxels)
         _check_params(kind, c, params)
         N.need_cuda("dirs", dirs, torch.float32)
@@ -167,7 +167,7 @@ class SegmentRender(Function):
             M = float(max(M, 1))
         reg_mean = reg.sum() / (float(B) * M)
         ctx.save_for_backward(voxels, params, dirs, pe_feat, pe_out, out4, rgb)
-        ctx.seg, ctx.kind, ctx.M, ctx.tc = seg, kind, M, tc
+        ctx.seg, ctx.kind, ctx.M, ctx.tc, ctx.grad_voxels = seg, kind, M, tc, grad_voxels
         return rgb, reg_mean
 
     @staticmethod
@@ -187,26 +187,36 @@ class SegmentRender(Function):
         d4 = torch.empty_like(out4)
         _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb),
                1.0 / B if scale is not None else 0.0, N.ptr(scale), N.ptr(d4), st)
-        gv = torch.zeros_like(voxels)
+        if ctx.grad_voxels is not None:
+            # caller-owned buffer, zero-filled on another stream while the
+            # forward ran; wait for that fill
+            gv, filled = ctx.grad_voxels
+            torch.cuda.current_stream(dev).wait_event(filled)
+        else:
+            gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
         if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st,
                                                   getattr(ctx, "saved_layers", None), out4):
-            return gv, gp, None, None, None, None, None, None, None
+            return gv, gp, None, None, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
-        return gv, gp, None, None, None, None, None, None, None
+        return gv, gp, None, None, None, None, None, None, None, None
 
 
 def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None,
-                    voxels16: torch.Tensor | None = None):
+                    voxels16: torch.Tensor | None = None, grad_voxels=None):
     """(rgb [B,3], sparsity term) for the CSR segments of B rays.  `tc` selects
     the tensor-core decoder; `voxels16` (inference) is a BF16/FP16 copy of the
-    grid the tensor-core forward reads its corner rows from."""
+    grid the tensor-core forward reads its corner rows from.  grad_voxels
+    (training, optional): (buffer, event) — a grid-shaped buffer that is all
+    zeros once `event` has completed; the grid gradient is accumulated into it
+    and returned as it, so its zero fill can overlap the forward."""
     # whether a backward will follow is known here, not inside the Function's
     # forward (which always runs with grad mode off): only then does the
     # tensor-core forward keep its layer tiles for the backward
     training = torch.is_grad_enabled() and (voxels.requires_grad or params.requires_grad)
-    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16, training)
+    return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16, training,
+                               grad_voxels)
 
 
 class DIVeRField(torch.nn.Module):
@@ -280,12 +290,14 @@ class DIVeRField(torch.nn.Module):
             self._g16key = key
         return self._g16
 
-    def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None):
+    def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None,
+                grad_voxels=None):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
         form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder).  Without
         autograd the tensor-core forms read a 16-bit copy of the grid.
-        capacity: fixed segment buffers, no host synchronisation (see segments)."""
+        capacity: fixed segment buffers, no host synchronisation (see segments).
+        grad_voxels: see render_segments."""
         seg = self.segments(os.contiguous(), ds.contiguous(), capacity)
         g16 = self.grid16(form) if not torch.is_grad_enabled() else None
         return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back,
-                               self.tc_weights(form), g16)
+                               self.tc_weights(form), g16, grad_voxels)
