@@ -347,7 +347,7 @@ def run_ours(args, rank, world, local):
         del field, step
         torch.cuda.empty_cache()
         extra = {"wide_train": run_wide_train(args, dev), "rt64_render": run_rt64_render(args, dev),
-                 "realtime_frame": run_realtime(args, dev)}
+                 "realtime_frame": run_realtime(args, dev), "prune": run_prune(args, dev)}
         torch.cuda.empty_cache()
     # ---- serving: 4 resident scenes, Poisson arrivals at 200 req/s ----
     serving = None
@@ -514,6 +514,38 @@ def run_realtime(args, dev):
             "host_loop": {"frame_ms": ms_loop, "rounds": rounds[-1],
                           "form": "aabb_intersect + rounds of ray_march / mlp_eval (the reference's loop)"},
             "features": int(ser["f"].shape[0])}
+
+
+def run_prune(args, dev):
+    """Occupancy extraction (prune.py:86-145) on the 256^3 x 32 DIVeR32 scene:
+    alpha map over 4 training views at 800x800 (2.56 M rays, batches of 65,536),
+    then the pruned mask at 1e-2 and the bias-sampling ray selection."""
+    import torch
+
+    from diver_gb300 import scenes
+    from diver_gb300.prune import extract_alpha_map, prune_mask, rays_hitting
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.grid_scene(256, 32, "diver32", device=dev)
+    field = DIVeRField.from_scene(sc, dev)
+    cams = scenes.sphere_cameras(100, 4.0, 3)
+    rays = torch.cat([torch.cat(scenes.camera_rays(cams[k], 800, 800, 960.0, dev), 1) for k in range(4)], 0)
+    extract_alpha_map(field, rays[:65536], batch=65536)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    alpha = extract_alpha_map(field, rays, batch=65536)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e)
+    mask = prune_mask(alpha)
+    s.record()
+    hit = rays_hitting(field, rays[:, :3], rays[:, 3:6], mask)
+    e.record()
+    torch.cuda.synchronize()
+    return {"rays": int(rays.shape[0]), "alpha_map_ms": ms, "Mrays_per_s": rays.shape[0] / (ms * 1e-3) / 1e6,
+            "kept_voxels": float(mask.float().mean().item()), "bias_sampling_ms": s.elapsed_time(e),
+            "rays_kept": float(hit.float().mean().item())}
 
 
 def run_serving(args, dev):

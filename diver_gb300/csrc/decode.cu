@@ -64,7 +64,15 @@ struct Kahan {
 // the reference's render (model/diver.py:295-319) with the transmittance kept
 // in log space (a compensated sum of relu(sigma), exact because
 // log(1 - alpha) = -relu(sigma)) instead of a running product.
-__global__ void __launch_bounds__(256) composite_fwd_kernel(const DecodeArgs a) {
+//
+// OCC: instead of colours, the per-segment weight w_i goes into an occupancy
+// map: alpha_map[cell] = max(alpha_map[cell], w_i) over the voxel cell
+// min(int(p0 + 1e-4), int(p1 + 1e-4)) of each segment whose cell lies in
+// [pad, N-1-pad]^3, flattened x + y N + z N^2 (prune.py:114-131, the
+// reference's torch_scatter max).  w_i >= 0, so the float maximum is an
+// integer atomicMax on the bit patterns of a map that starts at +0.
+template <bool OCC>
+__global__ void __launch_bounds__(256) composite_kernel(const DecodeArgs a) {
   const int ray = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (ray >= a.B) return;
@@ -80,12 +88,26 @@ __global__ void __launch_bounds__(256) composite_fwd_kernel(const DecodeArgs a) 
     const float excl = incl - s;
     const float T = expf(-(logt.s + excl) + logt.c);
     const float w = -expm1f(-s) * T;
+    if (OCC) {
+      if (valid) {
+        const float* p = a.seg + i * 6;
+        const int n = a.occ_n, lo = a.occ_pad, hi = a.occ_n - 1 - a.occ_pad;
+        const int cx = min((int)__fadd_rn(p[0], 1e-4f), (int)__fadd_rn(p[3], 1e-4f));
+        const int cy = min((int)__fadd_rn(p[1], 1e-4f), (int)__fadd_rn(p[4], 1e-4f));
+        const int cz = min((int)__fadd_rn(p[2], 1e-4f), (int)__fadd_rn(p[5], 1e-4f));
+        if (cx >= lo && cx <= hi && cy >= lo && cy <= hi && cz >= lo && cz <= hi)
+          atomicMax(reinterpret_cast<int*>(a.alpha_map) + ((long long)cz * n + cy) * n + cx, __float_as_int(w));
+      }
+      logt.add(__shfl_sync(0xffffffffu, incl, 31));
+      continue;
+    }
     r = fmaf(w, v.y, r);
     g = fmaf(w, v.z, g);
     bl = fmaf(w, v.w, bl);
     if (valid) reg += log1pf(v.x * v.x * 2.f);
     logt.add(__shfl_sync(0xffffffffu, incl, 31));
   }
+  if (OCC) return;
   r = warp_sum(r);
   g = warp_sum(g);
   bl = warp_sum(bl);
@@ -251,7 +273,25 @@ int dv_composite_fwd(int batch, const int64_t* offsets, const float* out4, int w
   a.rgb = rgb;
   a.t_final = t_final;
   a.reg_sum = reg_sum;
-  composite_fwd_kernel<<<ceil_div((long long)batch * 32, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  composite_kernel<false><<<ceil_div((long long)batch * 32, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_occupancy_max(int batch, const int64_t* offsets, const float* out4, const float* seg, int voxel_num, int pad,
+                     float* alpha_map, void* stream) {
+  DV_CHECK(batch >= 0 && voxel_num > 0 && pad >= 0, DV_ERR_ARG);
+  if (batch == 0) return DV_OK;
+  DV_CHECK(offsets && out4 && seg && alpha_map, DV_ERR_ARG);
+  DecodeArgs a{};
+  a.B = batch;
+  a.offsets = offsets;
+  a.out4 = reinterpret_cast<float4*>(const_cast<float*>(out4));
+  a.seg = seg;
+  a.occ_n = voxel_num;
+  a.occ_pad = pad;
+  a.alpha_map = alpha_map;
+  composite_kernel<true><<<ceil_div((long long)batch * 32, 256), 256, 0, (cudaStream_t)stream>>>(a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

@@ -51,6 +51,8 @@ struct DecodeArgs {
   const float* g_rgb;      // [B][3] dL/drgb
   float reg_coef;          // l_s / (B * M), or l_s / B with reg_scale = 1 / M
   const float* reg_scale;  // optional device factor on reg_coef
+  float* alpha_map;        // occupancy extraction: [N][N][N] max of segment weights
+  int occ_n, occ_pad;
 };
 
 // Layer indices: 0 .. D1-1 hidden layers of mlp1 (first: C -> W), D1: mlp1

@@ -290,6 +290,34 @@ class DIVeRField(torch.nn.Module):
             self._g16key = key
         return self._g16
 
+    @torch.no_grad()
+    def accumulate_alpha(self, os: torch.Tensor, ds: torch.Tensor, alpha_map: torch.Tensor, pad: int = 0,
+                         form: str = "fp32") -> None:
+        """alpha_map [N,N,N] (x fastest) = max(alpha_map, rendering weight) over
+        the voxels the rays' segments cross (prune.py:86-131)."""
+        N.need_cuda("alpha_map", alpha_map, torch.float32)
+        if alpha_map.numel() != self.voxel_num ** 3 or self.aniso:
+            raise ValueError("alpha_map must hold voxel_num^3 cells of a cubic grid")
+        os, ds = os.contiguous(), ds.contiguous()
+        seg = self.segments(os, ds)
+        if seg.total == 0:
+            return
+        nx, ny, nz, c = _grid(self.voxels)
+        kind = KIND_ID[self.kind]
+        dev, st, B = self.voxels.device, N.stream(self.voxels.device), ds.shape[0]
+        pe_feat = torch.empty(B, 28, device=dev)
+        pe_out = torch.empty(B, WIDTH[kind], device=dev)
+        _timed("dv_ray_pe", kind, c, N.ptr(self.params), B, N.ptr(ds), N.ptr(pe_feat), N.ptr(pe_out), st)
+        out4 = torch.empty(seg.total, 4, device=dev)
+        tc = self.tc_weights(form)
+        if tc is None:
+            _timed("dv_decode_fwd", kind, c, N.ptr(self.params), N.ptr(self.voxels), nx, ny, nz, N.ptr(seg.seg),
+                   N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_out), N.ptr(out4), st)
+        else:
+            tc.decode(kind, c, self.voxels, seg, pe_out, out4, st, self.grid16(form))
+        _timed("dv_occupancy_max", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(seg.seg), self.voxel_num, int(pad),
+               N.ptr(alpha_map), st)
+
     def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None,
                 grad_voxels=None):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).

@@ -208,6 +208,15 @@ DV_API int dv_decode_fwd(int kind, int channels, const float* params, const floa
 DV_API int dv_composite_fwd(int batch, const int64_t* offsets, const float* out4, int white_back,
                             float* rgb, float* t_final, float* reg_sum, void* stream);
 
+/* Occupancy extraction (prune.py:86-131): with the rendering weights
+ * w_i = alpha_i T_i of each ray's segments (out4 as from the decoder),
+ * alpha_map [N][N][N] (x fastest, caller-initialised, e.g. zeros) becomes
+ * max(alpha_map, w_i) at each segment's voxel min(int(p0 + 1e-4),
+ * int(p1 + 1e-4)) that lies in [pad, N-1-pad]^3 — the reference's
+ * torch_scatter max; voxel_mask = alpha_map > thresh is the pruned grid. */
+DV_API int dv_occupancy_max(int batch, const int64_t* offsets, const float* out4, const float* seg,
+                            int voxel_num, int pad, float* alpha_map, void* stream);
+
 /* d4 [n_seg][4] = (dL/dsigma_raw, dL/drgb_seg) from grad_rgb [batch][3];
  * reg_coef multiplies d/dsigma log(1 + sigma^2/0.5), and so does *reg_scale
  * (device float, optional: a factor known only on the device, e.g.
