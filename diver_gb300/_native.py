@@ -39,6 +39,9 @@ SIGNATURES = {
     "dv_exclusive_scan_static": (I32, [P, I64, P, P]),
     "dv_integrate_fwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_integrate_bwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
+    "dv_corner_rows": (I32, [P, P, I64, I64, I32, P, P]),
+    "dv_integrate_table_fwd": (I32, [P, I64, I32, P, P, P, I64, I64, P, P]),
+    "dv_integrate_table_bwd": (I32, [P, I64, I32, P, P, P, I64, I64, P, P]),
     "dv_decoder_param_count": (I32, [I32, I32]),
     "dv_ray_pe": (I32, [I32, I32, P, I32, P, P, P, P]),
     "dv_decode_fwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P]),

@@ -21,6 +21,7 @@ struct IntegrateArgs {
   const float* gin;    // backward: d feature [S][C]
   float* out;          // forward: feature [S][C]
   int nvx, nvy, nvz, C;
+  const int64_t* rows; // implicit stage: table row of each segment's 8 corners
 };
 
 __global__ void __launch_bounds__(256) integrate_fwd_kernel(const IntegrateArgs a) {
@@ -49,6 +50,70 @@ __global__ void __launch_bounds__(256) integrate_bwd_kernel(const IntegrateArgs 
                                        __ldg(po + 2), a.nvx, a.nvy, a.nvz);
   const float4 g = ldg4(a.gin + s * a.C + c4 * 4);
   scatter4(a.grad_grid, sc, a.C, c4, g, a.nvx, a.nvy);
+}
+
+// ---- implicit stage: features from a table of unique corners -------------
+// (utils/integrator.py:3-59).  rows [S][8]: the table row of each segment's
+// corner j (bit 0 = +x, bit 1 = +y, bit 2 = +z); the corner weights are those
+// of the explicit integral, from the segment's local coordinates.
+
+// rows[s][j] = linear index (z * nv + y) * nv + x of corner j, with the lower
+// corner min(int(p0 + 1e-4), int(p1 + 1e-4)) and the upper one clamped to
+// nv - 1 (utils/integrator.py:16-28).
+__global__ void __launch_bounds__(256) corner_rows_kernel(const float* __restrict__ ci, const float* __restrict__ co,
+                                                          long long stride, long long n_seg, int nv,
+                                                          int64_t* __restrict__ rows) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_seg) return;
+  const float* pi = ci + s * stride;
+  const float* po = co + s * stride;
+  int lo[3], hi[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = min((int)__fadd_rn(__ldg(pi + k), 1e-4f), (int)__fadd_rn(__ldg(po + k), 1e-4f));
+    hi[k] = min(lo[k] + 1, nv - 1);
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const long long x = (j & 1) ? hi[0] : lo[0], y = (j & 2) ? hi[1] : lo[1], z = (j & 4) ? hi[2] : lo[2];
+    rows[s * 8 + j] = (z * nv + y) * nv + x;
+  }
+}
+
+__global__ void __launch_bounds__(256) integrate_table_fwd_kernel(const IntegrateArgs a) {
+  const int tps = a.C >> 2;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long s = tid / tps;
+  const int c4 = (int)(tid - s * tps);
+  if (s >= a.n_seg) return;
+  const float* pi = a.ci + s * a.stride;
+  const float* po = a.co + s * a.stride;
+  const SegCorner sc = segment_corners(__ldg(pi), __ldg(pi + 1), __ldg(pi + 2), __ldg(po), __ldg(po + 1),
+                                       __ldg(po + 2), 1 << 30, 1 << 30, 1 << 30);
+  const int64_t* r = a.rows + s * 8;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) fma4(acc, sc.w[j], ldg4(a.grid + __ldg(r + j) * a.C + c4 * 4));
+  reinterpret_cast<float4*>(a.out + s * a.C)[c4] = acc;
+}
+
+__global__ void __launch_bounds__(256) integrate_table_bwd_kernel(const IntegrateArgs a) {
+  const int tps = a.C >> 2;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long s = tid / tps;
+  const int c4 = (int)(tid - s * tps);
+  if (s >= a.n_seg) return;
+  const float* pi = a.ci + s * a.stride;
+  const float* po = a.co + s * a.stride;
+  const SegCorner sc = segment_corners(__ldg(pi), __ldg(pi + 1), __ldg(pi + 2), __ldg(po), __ldg(po + 1),
+                                       __ldg(po + 2), 1 << 30, 1 << 30, 1 << 30);
+  const float4 g = ldg4(a.gin + s * a.C + c4 * 4);
+  const int64_t* r = a.rows + s * 8;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float w = sc.w[j];
+    red_add4(a.grad_grid + __ldg(r + j) * a.C + c4 * 4, make_float4(w * g.x, w * g.y, w * g.z, w * g.w));
+  }
 }
 
 static int check_common(const IntegrateArgs& a) {
@@ -108,6 +173,59 @@ int dv_integrate_bwd(const float* grad_feature, int nvx, int nvy, int nvz, int c
            DV_ERR_ARG);
   const long long threads = n_seg * (channels / 4);
   integrate_bwd_kernel<<<ceil_div(threads, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_corner_rows(const float* coord_i, const float* coord_o, long long coord_stride, long long n_seg, int n_vert,
+                   int64_t* rows, void* stream) {
+  DV_CHECK(n_seg >= 0 && n_vert > 0 && coord_stride >= 3, DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(coord_i && coord_o && rows, DV_ERR_ARG);
+  corner_rows_kernel<<<ceil_div(n_seg, 256), 256, 0, (cudaStream_t)stream>>>(coord_i, coord_o, coord_stride, n_seg,
+                                                                              n_vert, rows);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_integrate_table_fwd(const float* table, long long n_rows, int channels, const int64_t* rows,
+                           const float* coord_i, const float* coord_o, long long coord_stride, long long n_seg,
+                           float* feature, void* stream) {
+  DV_CHECK(n_seg >= 0 && n_rows >= 0 && channels > 0 && (channels & 3) == 0 && coord_stride >= 3, DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(table && rows && coord_i && coord_o && feature, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)table & 15) == 0 && ((uintptr_t)feature & 15) == 0, DV_ERR_ARG);
+  IntegrateArgs a{};
+  a.grid = table;
+  a.rows = rows;
+  a.ci = coord_i;
+  a.co = coord_o;
+  a.stride = coord_stride;
+  a.n_seg = n_seg;
+  a.out = feature;
+  a.C = channels;
+  integrate_table_fwd_kernel<<<ceil_div(n_seg * (channels / 4), 256), 256, 0, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_integrate_table_bwd(const float* grad_feature, long long n_rows, int channels, const int64_t* rows,
+                           const float* coord_i, const float* coord_o, long long coord_stride, long long n_seg,
+                           float* grad_table, void* stream) {
+  DV_CHECK(n_seg >= 0 && n_rows >= 0 && channels > 0 && (channels & 3) == 0 && coord_stride >= 3, DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(grad_feature && rows && coord_i && coord_o && grad_table, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)grad_table & 15) == 0 && ((uintptr_t)grad_feature & 15) == 0, DV_ERR_ARG);
+  IntegrateArgs a{};
+  a.grad_grid = grad_table;
+  a.rows = rows;
+  a.ci = coord_i;
+  a.co = coord_o;
+  a.stride = coord_stride;
+  a.n_seg = n_seg;
+  a.gin = grad_feature;
+  a.C = channels;
+  integrate_table_bwd_kernel<<<ceil_div(n_seg * (channels / 4), 256), 256, 0, (cudaStream_t)stream>>>(a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

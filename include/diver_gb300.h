@@ -174,6 +174,24 @@ DV_API int dv_integrate_bwd(const float* grad_feature, int nvx, int nvy, int nvz
                             const float* coord_i, const float* coord_o, long long coord_stride,
                             long long n_seg, float* grad_voxels, void* stream);
 
+/* Implicit stage (utils/integrator.py:3-59: integrate_mlp).  dv_corner_rows:
+ * rows [n_seg][8] int64, the linear index (z * n_vert + y) * n_vert + x of
+ * each segment's corner j (bit 0 = +x, bit 1 = +y, bit 2 = +z; lower corner
+ * min(int(p0 + 1e-4), int(p1 + 1e-4)), upper corner clamped to n_vert - 1).
+ * dv_integrate_table_fwd / _bwd: the integral of dv_integrate_fwd with corner
+ * j read from row rows[s][j] of a feature table [n_rows][channels] (the
+ * implicit MLP evaluated at the unique corners) instead of the grid; the
+ * backward accumulates into grad_table. */
+DV_API int dv_corner_rows(const float* coord_i, const float* coord_o, long long coord_stride,
+                          long long n_seg, int n_vert, int64_t* rows, void* stream);
+DV_API int dv_integrate_table_fwd(const float* table, long long n_rows, int channels,
+                                  const int64_t* rows, const float* coord_i, const float* coord_o,
+                                  long long coord_stride, long long n_seg, float* feature, void* stream);
+DV_API int dv_integrate_table_bwd(const float* grad_feature, long long n_rows, int channels,
+                                  const int64_t* rows, const float* coord_i, const float* coord_o,
+                                  long long coord_stride, long long n_seg, float* grad_table,
+                                  void* stream);
+
 /* ------------------------------------------------------------------------
  * Decoder + compositing, training/offline path (plain FP32).
  *

@@ -8,6 +8,9 @@ reference's training/offline decode path, used for reference gradients
   decode        model/diver.py:270-290 (mlp1 -> sigma, hidden; PE; mlp2; sigmoid)
   render        model/diver.py:295-319 (relu, 1-exp, shifted cumprod, white back)
   loss          train.py:84-85,109-113 (MSE + l_s * mean(log(1 + sigma^2 / 0.5)))
+  implicit_mlp  model/mlps.py:34-81 (PE of the vertex position, Linear+ReLU
+                layers with the encoded input re-joined before the skip layers,
+                a final Linear)
 
 Segment lists come in the CSR form (offsets, seg [S,6], ray [S]); the padded
 [B, M] layout of the reference is rebuilt here the way DIVeR.forward scatters
@@ -114,3 +117,14 @@ def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True,
 
 def loss(rgb, target, sigma, l_s=1e-5):
     return torch.nn.functional.mse_loss(rgb, target) + l_s * torch.log(1 + sigma ** 2 / 0.5).mean()
+
+
+def implicit_mlp(x: torch.Tensor, params: dict, depth: int, skips, enc: int) -> torch.Tensor:
+    """params: 'pts_linears.{i}.weight/bias' (i < depth) and 'feature_linear.weight/bias'."""
+    points = pos_enc(x, enc)
+    p = points
+    for i in range(depth):
+        if i in skips:
+            p = torch.cat([points, p], 1)
+        p = torch.relu(torch.nn.functional.linear(p, params[f"pts_linears.{i}.weight"], params[f"pts_linears.{i}.bias"]))
+    return torch.nn.functional.linear(p, params["feature_linear.weight"], params["feature_linear.bias"])
