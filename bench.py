@@ -347,7 +347,8 @@ def run_ours(args, rank, world, local):
         del field, step
         torch.cuda.empty_cache()
         extra = {"wide_train": run_wide_train(args, dev), "rt64_render": run_rt64_render(args, dev),
-                 "realtime_frame": run_realtime(args, dev), "prune": run_prune(args, dev)}
+                 "realtime_frame": run_realtime(args, dev), "prune": run_prune(args, dev),
+                 "implicit": run_implicit(args, dev)}
         torch.cuda.empty_cache()
     # ---- serving: 4 resident scenes, Poisson arrivals at 200 req/s ----
     serving = None
@@ -546,6 +547,44 @@ def run_prune(args, dev):
     return {"rays": int(rays.shape[0]), "alpha_map_ms": ms, "Mrays_per_s": rays.shape[0] / (ms * 1e-3) / 1e6,
             "kept_voxels": float(mask.float().mean().item()), "bias_sampling_ms": s.elapsed_time(e),
             "rays_kept": float(hit.float().mean().item())}
+
+
+def run_implicit(args, dev):
+    """Implicit stage (utils/integrator.py:3-59 + model/mlps.py:34-81): one
+    forward + backward of integrate_mlp over the segments of a 4096-ray training
+    batch of the 256^3 scene, ImplicitMLP(8, 512, [4], 32, 10) under BF16
+    autocast (its GEMMs are cuBLAS), gradients for the MLP."""
+    import torch
+
+    from diver_gb300 import scenes
+    from diver_gb300.implicit import ImplicitMLP
+    from diver_gb300.integrator import integrate_mlp
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.grid_scene(256, 32, "diver32", device=dev)
+    field = DIVeRField.from_scene(sc, dev)
+    o, d, _ = make_batches(sc, 1, dev)[0]
+    seg = field.segments(o, d)
+    del field
+    torch.manual_seed(0)
+    mlp = ImplicitMLP(8, 512, [4], 32, 10).to(dev)
+    G = torch.randn(seg.total, 32, device=dev)
+    uniq = {}
+
+    def step(i):
+        with torch.autocast("cuda", dtype=torch.bfloat16):
+            f = integrate_mlp(mlp, 257, 32, seg.seg[:, :3], seg.seg[:, 3:])
+        grads = torch.autograd.grad((f * G).sum(), list(mlp.parameters()))
+        return grads
+
+    ms = _time_steps(step, 2, 5)
+    from diver_gb300.integrator import corner_rows
+
+    U = int(torch.unique(corner_rows(seg.seg[:, :3], seg.seg[:, 3:], 257)).numel())
+    flops = 2 * 3 * U * (63 * 512 + 6 * 512 * 512 + (512 + 63) * 512 + 512 * 32)  # fwd + 2x bwd
+    return {"segments": seg.total, "unique_corners": U, "ms_per_step": ms,
+            "Mseg_per_s": seg.total / (ms * 1e-3) / 1e6, "mlp_tflops": flops / (ms * 1e-3) / 1e12,
+            "mlp": "ImplicitMLP(8, 512, [4], 32, 10), BF16 autocast (cuBLAS)"}
 
 
 def run_serving(args, dev):
