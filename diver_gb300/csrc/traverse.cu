@@ -401,6 +401,33 @@ __global__ void __launch_bounds__(256) march_kernel(int batch, float* __restrict
     march8<false>(coords, stride, b, last, d, mask, N);
 }
 
+// Pinhole camera rays (utils/dataset/ray_utils.py:5-55): pixel (i, j) looks
+// along ((i + 0.5 - W/2) / focal, -(j + 0.5 - H/2) / focal, -1), rotated by
+// the camera-to-world matrix and normalised; the origin is its translation.
+struct Camera {
+  float r[9];  // rotation, row-major (world = R * camera)
+  float t[3];
+  float focal;
+  int H, W;
+};
+
+__global__ void __launch_bounds__(256) camera_rays_kernel(const Camera c, float* __restrict__ o, float* __restrict__ d) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (long long)c.H * c.W) return;
+  const int j = (int)(p / c.W), i = (int)(p - (long long)j * c.W);
+  const float x = __fdiv_rn(__fsub_rn((float)i + 0.5f, 0.5f * (float)c.W), c.focal);
+  const float y = -__fdiv_rn(__fsub_rn((float)j + 0.5f, 0.5f * (float)c.H), c.focal);
+  float w[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) w[k] = fmaf(c.r[3 * k], x, fmaf(c.r[3 * k + 1], y, -c.r[3 * k + 2]));
+  const float n = sqrtf(fmaf(w[0], w[0], fmaf(w[1], w[1], w[2] * w[2])));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    d[3 * p + k] = __fdiv_rn(w[k], n);
+    o[3 * p + k] = c.t[k];
+  }
+}
+
 __global__ void pair_counts_kernel(int batch, const int* __restrict__ num, int* __restrict__ out) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < batch) out[b] = max(num[b] - 1, 0);
@@ -673,6 +700,22 @@ static WalkArgs walk_args_grid(int batch, const float* xyzmin, const int* dims, 
   a.v = v;
   a.mask = mask;
   return a;
+}
+
+int dv_camera_rays(int H, int W, float focal, const float* c2w, float* rays_o, float* rays_d, void* stream) {
+  DV_CHECK(H >= 0 && W >= 0 && c2w && (H == 0 || W == 0 || (rays_o && rays_d)), DV_ERR_ARG);
+  if ((long long)H * W == 0) return DV_OK;
+  Camera c{};
+  for (int k = 0; k < 3; ++k) {
+    for (int l = 0; l < 3; ++l) c.r[3 * k + l] = c2w[4 * k + l];
+    c.t[k] = c2w[4 * k + 3];
+  }
+  c.focal = focal;
+  c.H = H;
+  c.W = W;
+  camera_rays_kernel<<<ceil_div((long long)H * W, 256), 256, 0, (cudaStream_t)stream>>>(c, rays_o, rays_d);
+  DV_TRY_LAUNCH();
+  return DV_OK;
 }
 
 int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size, const float* o,

@@ -126,6 +126,19 @@ def camera_rays(c2w: torch.Tensor, H: int, W: int, focal: float, device="cpu"):
     return o.reshape(-1, 3).contiguous(), d.reshape(-1, 3).contiguous()
 
 
+def camera_rays_device(c2w: torch.Tensor, H: int, W: int, focal: float, device="cuda"):
+    """camera_rays generated on the device in one kernel (dv_camera_rays)."""
+    import ctypes
+
+    from . import _native as N
+
+    m = (ctypes.c_float * 12)(*[float(x) for x in c2w.float().reshape(-1).tolist()])
+    o = torch.empty(H * W, 3, device=device)
+    d = torch.empty(H * W, 3, device=device)
+    N.call("dv_camera_rays", H, W, float(focal), ctypes.addressof(m), N.ptr(o), N.ptr(d), N.stream(torch.device(device)))
+    return o, d
+
+
 def sphere_cameras(count: int, radius: float, seed: int) -> list[torch.Tensor]:
     g = _gen(seed, "cpu")
     v = torch.randn(count, 3, generator=g)

@@ -209,3 +209,17 @@ def test_bad_arguments_raise():
         masked_intersect(o, o, -1.0, 1.0, 8, 0.25, torch.ones(4, 4, 4, dtype=torch.bool, device="cuda"), 1.0)
     with pytest.raises(ValueError):
         masked_intersect(o.cpu(), o.cpu(), -1.0, 1.0, 8, 0.25, torch.ones(8, 8, 8, dtype=torch.bool), 1.0)
+
+
+@pytest.mark.gpu
+def test_camera_rays_on_device_match_reference_math():
+    """dv_camera_rays vs the reference's torch ray generation
+    (utils/dataset/ray_utils.py:5-55, restated in scenes.camera_rays): within
+    2e-7 abs (the matmul and norm reduce in a different order)."""
+    from diver_gb300 import scenes
+
+    c2w = scenes.sphere_cameras(3, 4.0, 3)[2]
+    o_ref, d_ref = scenes.camera_rays(c2w, 120, 160, 192.0, "cpu")
+    o, d = scenes.camera_rays_device(c2w, 120, 160, 192.0, "cuda")
+    assert torch.equal(o.cpu(), o_ref)
+    assert (d.cpu() - d_ref).abs().max().item() <= 2e-7
