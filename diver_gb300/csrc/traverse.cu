@@ -269,11 +269,11 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
   return count;
 }
 
-// 16 steps ahead when counting (few registers per step), 8 when the segments
-// are also written.
-template <int MODE>
+// K steps of lookahead: 16 for small batches (one warp per SM: registers are
+// plentiful and the occupancy-load latency is what is left), 8 otherwise
+// (the walk is issue-bound once several warps share a scheduler).
+template <int MODE, int K = 8>
 __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
-  constexpr int K = MODE == WALK_COUNT ? 16 : 8;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = b < a.batch;
   int count = 0;
@@ -287,6 +287,109 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
     if (MODE != WALK_SEGMENTS) a.num[b] = count;
   }
   if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
+}
+
+// Masked-walk emission for large batches, warp-staged.  The 32 rays of a
+// warp own consecutive CSR ranges, but each lane writing its own segments
+// scatters 32 stores per instruction across the output.  Here every lane
+// stages the (at most 8) segments of one lookahead batch in shared memory,
+// then the warp writes each lane's run with consecutive 4-byte stores (the
+// run of lane l is contiguous: seg[g..g+n)).  Same values, same places as the
+// direct writer; the walk arithmetic is the same masked walk.
+constexpr int STAGE_THREADS = 128;
+
+__device__ __forceinline__ void grid_step_sel(const float3 a, const float3 d, const float3 r, const float3 s, bool fast,
+                                              float3& b, float& dt) {
+  if (fast)
+    grid_step<true>(a, d, r, s, b, dt);
+  else
+    grid_step<false>(a, d, r, s, b, dt);
+}
+
+__global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const WalkArgs a) {
+  constexpr int K = 8;
+  __shared__ float stage[STAGE_THREADS * K * 8];  // per thread K segments x (6 coords, t, pad)
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int warp0 = threadIdx.x - lane;  // first thread of this warp in the block
+  float* mine = stage + threadIdx.x * K * 8;
+  bool done = true, fast = false;
+  float3 p = make_float3(0.f, 0.f, 0.f), d = p, r = p, sg = p;
+  float t = 0.f;
+  int64_t base = 0, cap = 0;
+  int count = 0;
+  if (b < a.batch) {
+    d = load3(a.v, b);
+    p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
+    if (box_entry3(p, d, a.n3, t)) {
+      done = false;
+      fast = a.fast && recip_ok(d);
+      r = fast ? recip3(d) : d;
+      sg = signs(d);
+      base = a.offsets[b];
+      cap = a.offsets[b + 1] - base;
+    }
+  }
+  while (__any_sync(0xffffffffu, !done)) {
+    int nb = 0;
+    const int64_t g = base + (count < cap ? count : cap);  // where this batch's first segment goes
+    if (!done) {
+      float3 P[K + 1];
+      float T[K];
+      uint8_t occ[K];
+      unsigned inb = 0;
+      P[0] = p;
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (!done) {
+          float3 q;
+          float dt;
+          grid_step_sel(P[k], d, r, sg, fast, q, dt);
+          t = __fadd_rn(t, dt);
+          if (outside_closed3(q, a.n3)) {
+            done = true;
+          } else {
+            P[k + 1] = q;
+            T[k] = t;
+            const long long idx = cell_index3(P[k], q, a.mask_scale, a.mx, a.my);
+            const bool in_mask = idx >= 0 && idx < a.cells;
+            occ[k] = __ldg(a.mask + (in_mask ? idx : 0));
+            inb |= (in_mask ? 1u : 0u) << k;
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        if (((inb >> k) & 1u) && occ[k] != 0) {
+          if (count < cap) {
+            float4* slot = reinterpret_cast<float4*>(mine + nb * 8);
+            slot[0] = make_float4(P[k].x, P[k].y, P[k].z, P[k + 1].x);
+            slot[1] = make_float4(P[k + 1].y, P[k + 1].z, __fmul_rn(T[k], a.voxel_size), 0.f);
+            ++nb;
+          }
+          ++count;
+        }
+      }
+      p = P[K];
+    }
+    __syncwarp();
+    unsigned pending = __ballot_sync(0xffffffffu, nb > 0);
+    while (pending) {
+      const int l = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const int n = __shfl_sync(0xffffffffu, nb, l);
+      const long long gl = (long long)(((unsigned long long)(unsigned)__shfl_sync(0xffffffffu, (int)(g >> 32), l) << 32) |
+                                       (unsigned)__shfl_sync(0xffffffffu, (int)(g & 0xffffffffu), l));
+      const float* src = stage + (warp0 + l) * K * 8;
+      for (int w = lane; w < n * 6; w += 32) {
+        const int k = w / 6;
+        a.seg[gl * 6 + w] = src[k * 8 + (w - k * 6)];
+      }
+      if (a.seg_t && lane < n) a.seg_t[gl + lane] = src[lane * 8 + 6];
+      if (a.seg_ray && lane < n) a.seg_ray[gl + lane] = blockIdx.x * blockDim.x + warp0 + l;
+    }
+    __syncwarp();
+  }
 }
 
 // Octree first hit.  Reference ray_march.cu:33-148, generalised from the
@@ -537,6 +640,15 @@ static int walk_block(int batch) {
   return batch < sms * 256 ? 32 : 256;
 }
 
+#define DV_COUNT_LAUNCH(batch, stream, args)                                                      \
+  do {                                                                                              \
+    const int bs__ = walk_block(batch);                                                             \
+    if (bs__ == 32)                                                                                 \
+      masked_walk_kernel<WALK_COUNT, 16><<<ceil_div((batch), bs__), bs__, 0, (cudaStream_t)(stream)>>>(args); \
+    else                                                                                            \
+      masked_walk_kernel<WALK_COUNT, 8><<<ceil_div((batch), bs__), bs__, 0, (cudaStream_t)(stream)>>>(args);  \
+  } while (0)
+
 #define DV_WALK_LAUNCH(kernel, batch, stream, args)                              \
   do {                                                                             \
     const int bs__ = walk_block(batch);                                            \
@@ -633,7 +745,7 @@ int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_s
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
-  DV_WALK_LAUNCH(masked_walk_kernel<WALK_COUNT>, batch_size, stream, a);
+  DV_COUNT_LAUNCH(batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -651,7 +763,10 @@ int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxe
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
-  DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
+  if (walk_block(batch_size) == 256)
+    masked_emit_staged_kernel<<<ceil_div(batch_size, STAGE_THREADS), STAGE_THREADS, 0, (cudaStream_t)stream>>>(a);
+  else
+    DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -726,7 +841,7 @@ int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, f
   WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
-  DV_WALK_LAUNCH(masked_walk_kernel<WALK_COUNT>, batch_size, stream, a);
+  DV_COUNT_LAUNCH(batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }
@@ -743,7 +858,10 @@ int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
-  DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
+  if (walk_block(batch_size) == 256)
+    masked_emit_staged_kernel<<<ceil_div(batch_size, STAGE_THREADS), STAGE_THREADS, 0, (cudaStream_t)stream>>>(a);
+  else
+    DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

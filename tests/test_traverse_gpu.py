@@ -223,3 +223,28 @@ def test_camera_rays_on_device_match_reference_math():
     o, d = scenes.camera_rays_device(c2w, 120, 160, 192.0, "cuda")
     assert torch.equal(o.cpu(), o_ref)
     assert (d.cpu() - d_ref).abs().max().item() <= 2e-7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_rays", [3000, 60000])
+def test_masked_segments_both_writers_bit_exact(n_rays):
+    """Small batches write segments per lane, large ones stage them per warp
+    (masked_emit_staged_kernel): both give the oracle's CSR lists bit for bit."""
+    from diver_gb300 import masked_segments, scenes
+
+    sc = scenes.small_scene("cpu")
+    o, v = scenes.small_view("cpu")
+    g = torch.Generator().manual_seed(n_rays)
+    pick = torch.randint(0, o.shape[0], (n_rays,), generator=g)
+    jitter = (torch.rand(n_rays, 3, generator=g) - 0.5) * 0.2
+    v = v[pick] + jitter
+    v = (v / v.norm(dim=1, keepdim=True)).contiguous()
+    o = o[pick].contiguous()
+    seg = masked_segments(o.cuda(), v.cuda(), sc.xyzmin, sc.voxel_num, sc.voxel_size, sc.mask.cuda(), 1.0)
+    inter, num, tns = orc.masked_walk(o.numpy(), v.numpy(), sc.xyzmin, sc.voxel_num, sc.voxel_size, sc.mask.numpy(),
+                                      1.0)
+    ref = orc.csr_from_padded(inter, num)
+    ref_t = orc.csr_from_padded(tns[..., None], num)[:, 0]
+    assert same_bits(seg.seg.cpu().numpy(), ref)
+    assert same_bits(seg.t.cpu().numpy(), ref_t)
+    assert np.array_equal(seg.ray.cpu().numpy(), np.repeat(np.arange(n_rays), num))
