@@ -33,7 +33,7 @@ SIGNATURES = {
     "dv_masked_segments_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P, P]),
     "dv_dense_segments": (I32, [I32, F32, F32, F32, P, P, P, P, P, P, P]),
     "dv_dense_pair_counts": (I32, [I32, P, P, P]),
-    "dv_camera_rays": (I32, [I32, I32, F32, P, P, P, P]),
+    "dv_camera_rays": (I32, [I32, I32, F32, P, I64, I64, P, P, P]),
     "dv_scan_scratch_bytes": (I64, [I64]),
     "dv_exclusive_scan": (I32, [P, I64, P, P, P]),
     "dv_exclusive_scan_static_max": (I64, []),

@@ -512,12 +512,14 @@ struct Camera {
   float t[3];
   float focal;
   int H, W;
+  long long first, count;  // pixel range [first, first + count) of the H x W image
 };
 
 __global__ void __launch_bounds__(256) camera_rays_kernel(const Camera c, float* __restrict__ o, float* __restrict__ d) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= (long long)c.H * c.W) return;
-  const int j = (int)(p / c.W), i = (int)(p - (long long)j * c.W);
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // output row
+  if (p >= c.count) return;
+  const long long px = c.first + p;
+  const int j = (int)(px / c.W), i = (int)(px - (long long)j * c.W);
   const float x = __fdiv_rn(__fsub_rn((float)i + 0.5f, 0.5f * (float)c.W), c.focal);
   const float y = -__fdiv_rn(__fsub_rn((float)j + 0.5f, 0.5f * (float)c.H), c.focal);
   float w[3];
@@ -817,9 +819,12 @@ static WalkArgs walk_args_grid(int batch, const float* xyzmin, const int* dims, 
   return a;
 }
 
-int dv_camera_rays(int H, int W, float focal, const float* c2w, float* rays_o, float* rays_d, void* stream) {
-  DV_CHECK(H >= 0 && W >= 0 && c2w && (H == 0 || W == 0 || (rays_o && rays_d)), DV_ERR_ARG);
-  if ((long long)H * W == 0) return DV_OK;
+int dv_camera_rays(int H, int W, float focal, const float* c2w, long long first_pixel, long long n_pixels,
+                   float* rays_o, float* rays_d, void* stream) {
+  DV_CHECK(H >= 0 && W >= 0 && c2w && first_pixel >= 0 && n_pixels >= 0, DV_ERR_ARG);
+  DV_CHECK(first_pixel + n_pixels <= (long long)H * W, DV_ERR_ARG);
+  if (n_pixels == 0) return DV_OK;
+  DV_CHECK(rays_o && rays_d, DV_ERR_ARG);
   Camera c{};
   for (int k = 0; k < 3; ++k) {
     for (int l = 0; l < 3; ++l) c.r[3 * k + l] = c2w[4 * k + l];
@@ -828,7 +833,9 @@ int dv_camera_rays(int H, int W, float focal, const float* c2w, float* rays_o, f
   c.focal = focal;
   c.H = H;
   c.W = W;
-  camera_rays_kernel<<<ceil_div((long long)H * W, 256), 256, 0, (cudaStream_t)stream>>>(c, rays_o, rays_d);
+  c.first = first_pixel;
+  c.count = n_pixels;
+  camera_rays_kernel<<<ceil_div(n_pixels, 256), 256, 0, (cudaStream_t)stream>>>(c, rays_o, rays_d);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

@@ -126,16 +126,20 @@ def camera_rays(c2w: torch.Tensor, H: int, W: int, focal: float, device="cpu"):
     return o.reshape(-1, 3).contiguous(), d.reshape(-1, 3).contiguous()
 
 
-def camera_rays_device(c2w: torch.Tensor, H: int, W: int, focal: float, device="cuda"):
-    """camera_rays generated on the device in one kernel (dv_camera_rays)."""
+def camera_rays_device(c2w: torch.Tensor, H: int, W: int, focal: float, device="cuda", first: int = 0,
+                       count: int | None = None):
+    """camera_rays generated on the device in one kernel (dv_camera_rays), for
+    pixels [first, first + count) of the row-major image (all by default)."""
     import ctypes
 
     from . import _native as N
 
+    n = H * W - first if count is None else int(count)
     m = (ctypes.c_float * 12)(*[float(x) for x in c2w.float().reshape(-1).tolist()])
-    o = torch.empty(H * W, 3, device=device)
-    d = torch.empty(H * W, 3, device=device)
-    N.call("dv_camera_rays", H, W, float(focal), ctypes.addressof(m), N.ptr(o), N.ptr(d), N.stream(torch.device(device)))
+    o = torch.empty(n, 3, device=device)
+    d = torch.empty(n, 3, device=device)
+    N.call("dv_camera_rays", H, W, float(focal), ctypes.addressof(m), int(first), n, N.ptr(o), N.ptr(d),
+           N.stream(torch.device(device)))
     return o, d
 
 

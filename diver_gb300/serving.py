@@ -195,16 +195,10 @@ class GpuRenderer:
 
     @staticmethod
     def rays_for(req: Request, first: int, count: int, device):
-        from .scenes import pixel_directions
+        """The chunk's camera rays, generated on the device for its pixels only."""
+        from .scenes import camera_rays_device
 
-        idx = torch.arange(first, first + count, device=device)
-        j, i = idx // req.width, idx % req.width
-        dirs = pixel_directions(req.height, req.width, req.focal, device).reshape(-1, 3)[idx]
-        c2w = req.c2w.to(device)
-        d = dirs @ c2w[:, :3].t()
-        d = d / d.norm(dim=-1, keepdim=True)
-        o = c2w[:, 3].expand(d.shape)
-        return o.contiguous(), d.contiguous()
+        return camera_rays_device(req.c2w, req.height, req.width, req.focal, device, first, count)
 
     def render(self, field_model, work: list[tuple[Request, int, int]]):
         """Launches one batch for all chunks in `work` on the scene's stream; returns

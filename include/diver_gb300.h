@@ -315,11 +315,12 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
                             long long saved_bytes, const float* out4, float* grad_voxels,
                             float* grad_params, int* err, void* stream);
 
-/* Pinhole camera rays of an H x W image (utils/dataset/ray_utils.py:5-55):
- * rays_o / rays_d [H*W][3] (device), row-major pixels; c2w is a HOST float
- * [3][4] camera-to-world matrix; directions unit length. */
-DV_API int dv_camera_rays(int H, int W, float focal, const float* c2w, float* rays_o, float* rays_d,
-                          void* stream);
+/* Pinhole camera rays of pixels [first_pixel, first_pixel + n_pixels) of an
+ * H x W image, row-major (utils/dataset/ray_utils.py:5-55): rays_o / rays_d
+ * [n_pixels][3] (device); c2w is a HOST float [3][4] camera-to-world matrix;
+ * directions unit length. */
+DV_API int dv_camera_rays(int H, int W, float focal, const float* c2w, long long first_pixel,
+                          long long n_pixels, float* rays_o, float* rays_d, void* stream);
 
 /* ------------------------------------------------------------------------
  * Real-time path: occupancy-octree first hit and 8-hit ray march.

@@ -223,6 +223,8 @@ def test_camera_rays_on_device_match_reference_math():
     o, d = scenes.camera_rays_device(c2w, 120, 160, 192.0, "cuda")
     assert torch.equal(o.cpu(), o_ref)
     assert (d.cpu() - d_ref).abs().max().item() <= 2e-7
+    o2, d2 = scenes.camera_rays_device(c2w, 120, 160, 192.0, "cuda", 5000, 3000)  # a pixel range
+    assert torch.equal(d2, d[5000:8000]) and torch.equal(o2, o[5000:8000])
 
 
 @pytest.mark.gpu
