@@ -107,13 +107,20 @@ def barrier(world):
         dist.barrier()
 
 
+def _reduce_device() -> str:
+    """Where the timing reductions live: the GPU for NCCL, the host for gloo."""
+    import torch.distributed as dist
+
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def allreduce_max(x: float, world: int) -> float:
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    t = torch.tensor([x], device=_reduce_device(), dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -124,7 +131,7 @@ def allreduce_sum(x: float, world: int) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    t = torch.tensor([x], device=_reduce_device(), dtype=torch.float64)
     dist.all_reduce(t)
     return float(t.item())
 
