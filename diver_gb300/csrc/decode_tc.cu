@@ -329,6 +329,21 @@ int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   return DV_OK;
 }
 
+// Exercises the bounded completion wait that every tensor-core kernel uses
+// (tc::mbar_wait_bounded): one wait on an mbarrier that nobody arrives on
+// must give up after `limit` polls and report it; one after an arrival must
+// succeed.  status[0] = 1 if the unarrived wait timed out, status[1] = 0 if
+// the arrived wait completed.
+__global__ void wait_selftest_kernel(uint32_t limit, int* status) {
+  __shared__ __align__(8) uint64_t bar[2];
+  tc::mbar_init(&bar[0], 1);
+  tc::mbar_init(&bar[1], 1);
+  tc::fence_mbar_init();
+  status[0] = tc::mbar_wait_bounded(&bar[0], 0, limit) ? 0 : 1;
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(&bar[1])) : "memory");
+  status[1] = tc::mbar_wait_bounded(&bar[1], 0, limit) ? 0 : 1;
+}
+
 }  // namespace dv
 
 using namespace dv;
@@ -400,6 +415,13 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
   if (channels == 32)
     return bf16 ? launch_decode_fwd_tc<32, 64, 1, 1>(a, st) : launch_decode_fwd_tc<32, 64, 1, 0>(a, st);
   return bf16 ? launch_decode_fwd_tc<64, 64, 1, 1>(a, st) : launch_decode_fwd_tc<64, 64, 1, 0>(a, st);
+}
+
+int dv_wait_selftest(int limit, int* status, void* stream) {
+  DV_CHECK(limit > 0 && limit <= (1 << 20) && status, DV_ERR_ARG);
+  wait_selftest_kernel<<<1, 1, 0, (cudaStream_t)stream>>>((uint32_t)limit, status);
+  DV_TRY_LAUNCH();
+  return DV_OK;
 }
 
 long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg) {

@@ -271,6 +271,14 @@ DV_API int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob,
                             const int64_t* n_seg_dev, const float* pe_out, float* out4, void* save,
                             long long save_capacity, int* err, void* stream);
 
+/* Self-test of the bounded completion waits of the tensor-core kernels (no
+ * counterpart in the reference): status (device int[2]) gets status[0] = 1
+ * when a wait on an mbarrier that nobody arrives on gave up after `limit`
+ * polls (at most 2^20), status[1] = 0 when a wait after an arrival completed.
+ * The kernels report such a timeout through their `err` word and stop
+ * issuing work; nothing spins unbounded. */
+DV_API int dv_wait_selftest(int limit, int* status, void* stream);
+
 /* Bytes of the `save` buffer of dv_decode_fwd_tc for n_seg segments: per
  * tile of 128 segments, every layer's input tile (BF16/FP16, the K-major
  * operand layout) in layer order; dv_decode_bwd_tc reads them back instead

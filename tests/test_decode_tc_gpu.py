@@ -252,3 +252,16 @@ def test_inference_render_keeps_no_layer_tiles(monkeypatch):
         rgb, _ = field(o.cuda(), v.cuda(), form="bf16")
     torch.cuda.synchronize()
     assert torch.isfinite(rgb).all()
+
+
+def test_bounded_wait_reports_a_timeout_and_completes_after_arrival():
+    """Failure detection without a fault: a completion wait that nothing
+    satisfies gives up after its poll limit and says so; the context stays
+    usable (the next call on it works)."""
+    from diver_gb300 import _native as N
+
+    status = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    N.call("dv_wait_selftest", 1000, N.ptr(status), N.stream())
+    torch.cuda.synchronize()
+    assert status.tolist() == [1, 0]
+    assert torch.ones(4, device="cuda").sum().item() == 4.0
