@@ -237,6 +237,9 @@ def serve(requests: list[Request], residency: Residency, renderer: GpuRenderer, 
     while not sch.idle():
         now = time.perf_counter() - t0 if realtime else float("inf")
         sch.admit(now)
+        if not sch.active and sch.waiting and not inflight:
+            # with nothing running, admission only fails when the scene cannot fit the budget
+            raise RuntimeError("requests cannot be admitted: scene larger than the free HBM budget")
         batches = sch.next_batches()
         for scene, work in batches.items():
             model = residency.scenes[scene].resident
@@ -253,8 +256,6 @@ def serve(requests: list[Request], residency: Residency, renderer: GpuRenderer, 
             else:
                 still.append((ev, out))
         inflight = still
-        if not batches and not inflight and sch.active == [] and sch.waiting and not sch.arrivals:
-            raise RuntimeError("requests cannot be admitted: scene larger than the free HBM budget")
         if realtime and not batches and not inflight:
             nxt = sch.next_arrival()
             if nxt is not None:

@@ -79,6 +79,47 @@ def test_request_waits_for_ray_slots():
     assert sch.active == [b]
 
 
+class LateDone:
+    """A batch that completes only after the loop has polled it once."""
+
+    def __init__(self):
+        self.polls = 0
+
+    def query(self):
+        self.polls += 1
+        return self.polls > 1
+
+    def synchronize(self):
+        self.polls = 1
+
+
+class OneChunkRenderer:
+    def render(self, model, work):
+        return LateDone(), work
+
+
+def test_waiting_requests_are_admitted_after_the_active_ones_finish():
+    """Ray slots (not the HBM budget) hold a request back; when the last active
+    request retires in an iteration that issued no batch, the waiting one is
+    admitted on the next pass instead of being reported as unadmittable."""
+    res = Residency(100)
+    res.register("s", 1, lambda: "m")
+    c2w = torch.eye(4)[:3]
+    reqs = [Request(i, "s", c2w, 4, 5, 1.0, arrival=0.0) for i in range(3)]  # 20 rays each
+    done = serve(reqs, res, OneChunkRenderer(), realtime=False, max_rays_in_flight=20, chunk_rays=100)
+    assert sorted(r.rid for r in done) == [0, 1, 2]
+
+
+def test_a_scene_larger_than_the_free_budget_is_reported():
+    res = Residency(10)
+    res.register("a", 8, lambda: "A")
+    res.register("b", 8, lambda: "B")
+    assert res.acquire("a")  # held by someone else for the whole run
+    c2w = torch.eye(4)[:3]
+    with pytest.raises(RuntimeError):
+        serve([Request(0, "b", c2w, 2, 2, 1.0)], res, FakeRenderer(), realtime=False)
+
+
 @pytest.mark.gpu
 def test_same_result_alone_and_in_the_mix():
     from diver_gb300 import scenes
