@@ -27,10 +27,10 @@ SIGNATURES = {
     "dv_ray_voxel_intersect": (I32, [I32, I32, F32, F32, F32, F32, P, P, P, P, P, P, P]),
     "dv_ray_voxel_count": (I32, [I32, F32, F32, F32, P, P, P, P, P]),
     "dv_masked_intersect": (I32, [I32, I32, F32, F32, F32, F32, F32, P, P, P, P, P, P, P, P]),
-    "dv_masked_count": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P]),
-    "dv_masked_segments": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P, P, P]),
-    "dv_masked_count_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P]),
-    "dv_masked_segments_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P, P]),
+    "dv_masked_count": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P, P]),
+    "dv_masked_segments": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P, P, P, P]),
+    "dv_masked_count_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P]),
+    "dv_masked_segments_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P, P, P]),
     "dv_dense_segments": (I32, [I32, F32, F32, F32, P, P, P, P, P, P, P]),
     "dv_dense_pair_counts": (I32, [I32, P, P, P]),
     "dv_camera_rays": (I32, [I32, I32, F32, P, I64, I64, P, P, P]),

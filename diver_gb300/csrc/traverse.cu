@@ -36,6 +36,8 @@ struct WalkArgs {
   int* num;
   float* tns;
   int* max_count;
+  int* last_step;          // count: per ray, the walk step (1-based) of its last occupied voxel, 0 if none
+  const int* stop_step;    // segments: per ray, the step after which the walk may stop (last_step of the count)
   const int64_t* offsets;
   float* seg;
   float* seg_t;
@@ -218,15 +220,22 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
   SegWriter w;
   int count = 0;
   bool done = false;
+  // steps taken so far, the step of the last occupied voxel (counting), and
+  // where the walk may stop (emitting: nothing occupied lies beyond it)
+  int steps = 0, last = 0;
+  const int limit = (MODE == WALK_SEGMENTS && a.stop_step) ? a.stop_step[b] : 0x7fffffff;
   while (!done) {
     float3 P[LOOKAHEAD + 1];
     float T[LOOKAHEAD];
     uint8_t occ[LOOKAHEAD];
     unsigned inb = 0;  // bit k: step k stayed in the box and its cell is inside the mask
+    const int first = steps;
     P[0] = p;
 #pragma unroll
     for (int k = 0; k < LOOKAHEAD; ++k) {
+      if (!done && steps >= limit) done = true;
       if (!done) {
+        ++steps;
         float3 q;
         float dt;
         grid_step<FAST>(P[k], d, r, s, q, dt);
@@ -248,6 +257,7 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
 #pragma unroll
     for (int k = 0; k < LOOKAHEAD; ++k) {
       if (((inb >> k) & 1u) && occ[k] != 0) {
+        last = first + k + 1;
         if (MODE == WALK_PADDED && count < a.max_n) {
           float* rr = row + 6 * count;
           rr[0] = P[k].x;
@@ -266,6 +276,7 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
     p = P[LOOKAHEAD];  // only read again when all LOOKAHEAD steps stayed inside
   }
   if (MODE == WALK_SEGMENTS) w.flush(a, b);
+  if (MODE == WALK_COUNT && a.last_step) a.last_step[b] = last;
   return count;
 }
 
@@ -284,6 +295,8 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
     if (box_entry3(p, d, a.n3, t))
       count = (a.fast && recip_ok(d)) ? masked_walk<MODE, true, K>(a, b, p, d, t)
                                       : masked_walk<MODE, false, K>(a, b, p, d, t);
+    else if (MODE == WALK_COUNT && a.last_step)
+      a.last_step[b] = 0;
     if (MODE != WALK_SEGMENTS) a.num[b] = count;
   }
   if (MODE != WALK_SEGMENTS) warp_max_atomic(a.max_count, count, live);
@@ -337,6 +350,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
   }
   int nb = 0;         // staged segments of this lane
   int64_t g = base;   // global index of the first staged one
+  int steps = 0;      // walk steps taken; nothing occupied lies beyond `limit`
+  const int limit = (!done && a.stop_step) ? a.stop_step[b] : 0x7fffffff;
   while (__any_sync(0xffffffffu, !done) || __any_sync(0xffffffffu, nb > 0)) {
     if (!done) {
       float3 P[K + 1];
@@ -346,7 +361,9 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
       P[0] = p;
 #pragma unroll
       for (int k = 0; k < K; ++k) {
+        if (!done && steps >= limit) done = true;
         if (!done) {
+          ++steps;
           float3 q;
           float dt;
           grid_step_sel(P[k], d, r, sg, fast, q, dt);
@@ -751,13 +768,14 @@ int dv_masked_intersect(int batch_size, int max_n, float xyzmin, float xyzmax, f
 
 int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
                     float mask_scale, const float* o, const float* v, const uint8_t* mask,
-                    int* intersect_num, int* max_count, void* stream) {
+                    int* intersect_num, int* max_count, int* last_step, void* stream) {
   DV_CHECK(batch_size >= 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && intersect_num, DV_ERR_ARG);
   WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
+  a.last_step = last_step;
   DV_COUNT_LAUNCH(batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
@@ -766,7 +784,7 @@ int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_s
 int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
                        float mask_scale, const float* o, const float* v, const uint8_t* mask,
                        const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
-                       void* stream) {
+                       const int* stop_step, void* stream) {
   DV_CHECK(batch_size >= 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
@@ -776,6 +794,7 @@ int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxe
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
+  a.stop_step = stop_step;
   if (walk_block(batch_size) == 256)
     masked_emit_staged_kernel<<<ceil_div(batch_size, STAGE_THREADS), STAGE_THREADS, 0, (cudaStream_t)stream>>>(a);
   else
@@ -852,13 +871,15 @@ int dv_camera_rays(int H, int W, float focal, const float* c2w, long long first_
 }
 
 int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size, const float* o,
-                         const float* v, const uint8_t* mask, int* intersect_num, int* max_count, void* stream) {
+                         const float* v, const uint8_t* mask, int* intersect_num, int* max_count, int* last_step,
+                         void* stream) {
   DV_CHECK(batch_size >= 0 && xyzmin && dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && intersect_num, DV_ERR_ARG);
   WalkArgs a = walk_args_grid(batch_size, xyzmin, dims, voxel_size, o, v, mask);
   a.num = intersect_num;
   a.max_count = max_count;
+  a.last_step = last_step;
   DV_COUNT_LAUNCH(batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
@@ -866,7 +887,7 @@ int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, f
 
 int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size, const float* o,
                             const float* v, const uint8_t* mask, const int64_t* offsets, float* seg, float* seg_t,
-                            int* seg_ray, void* stream) {
+                            int* seg_ray, const int* stop_step, void* stream) {
   DV_CHECK(batch_size >= 0 && xyzmin && dims && dims[0] > 0 && dims[1] > 0 && dims[2] > 0, DV_ERR_ARG);
   if (batch_size == 0) return DV_OK;
   DV_CHECK(o && v && mask && offsets && seg, DV_ERR_ARG);
@@ -876,6 +897,7 @@ int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims
   a.seg = seg;
   a.seg_t = seg_t;
   a.seg_ray = seg_ray;
+  a.stop_step = stop_step;
   if (walk_block(batch_size) == 256)
     masked_emit_staged_kernel<<<ceil_div(batch_size, STAGE_THREADS), STAGE_THREADS, 0, (cudaStream_t)stream>>>(a);
   else

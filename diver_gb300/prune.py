@@ -49,5 +49,5 @@ def rays_hitting(field: DIVeRField, o: torch.Tensor, d: torch.Tensor, voxel_mask
     num = torch.empty(B, dtype=torch.int32, device=o.device)
     if B:
         N.call("dv_masked_count", B, float(field.xyzmin), float(field.voxel_num), float(field.voxel_size),
-               float(mask_scale), N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, N.stream(o.device))
+               float(mask_scale), N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, None, N.stream(o.device))
     return num > 0

@@ -87,7 +87,7 @@ class MaskedIntersect(Function):
         num = torch.empty(B, dtype=torch.int32, device=dev)
         mx = torch.zeros(1, dtype=torch.int32, device=dev)
         N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), st)
+               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), None, st)
         K = _max_count(mx)
         inter = torch.zeros(B, K, 6, dtype=torch.float32, device=dev)
         tns = torch.full((B, K), -1.0, dtype=torch.float32, device=dev)
@@ -187,9 +187,10 @@ def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capac
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
+    last = torch.empty(B, dtype=torch.int32, device=dev)  # where each ray's emission walk may stop
     mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), st)
+           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), N.ptr(last), st)
     offsets = exclusive_scan(num)
     if capacity is None:
         S, M = _totals(offsets, num)
@@ -198,7 +199,7 @@ def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capac
     seg, t, ray = _buffers(S, dev)
     if S > 0 and B > 0:
         N.call("dv_masked_segments", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
+               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), N.ptr(last), st)
     return Segments(offsets, seg, t, ray, num, M, mx)
 
 
@@ -246,9 +247,10 @@ def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask, capacity: int | N
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
+    last = torch.empty(B, dtype=torch.int32, device=dev)
     mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o), N.ptr(v),
-           N.ptr(m8), N.ptr(num), N.ptr(mx), st)
+           N.ptr(m8), N.ptr(num), N.ptr(mx), N.ptr(last), st)
     offsets = exclusive_scan(num)
     if capacity is None:
         S, M = _totals(offsets, num)
@@ -257,5 +259,5 @@ def masked_segments_grid(o, v, xyzmin, dims, voxel_size, mask, capacity: int | N
     seg, t, ray = _buffers(S, dev)
     if S > 0 and B > 0:
         N.call("dv_masked_segments_grid", B, ctypes.addressof(x0), ctypes.addressof(dd), float(voxel_size), N.ptr(o),
-               N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), st)
+               N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), N.ptr(last), st)
     return Segments(offsets, seg, t, ray, num, M, mx)

@@ -264,7 +264,7 @@ def training_batches(scene: Scene, count: int, batch: int, device, seed: int = 4
         o = c2w[:, 3].expand(d.shape).contiguous()
         num = torch.empty(d.shape[0], dtype=torch.int32, device=device)
         N.call("dv_masked_count", d.shape[0], scene.xyzmin, float(scene.voxel_num), scene.voxel_size, 1.0,
-               N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, N.stream(device))
+               N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, None, N.stream(device))
         keep = torch.nonzero(num > 0)[:, 0]
         if keep.numel() < batch:
             continue

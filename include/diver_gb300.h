@@ -91,9 +91,13 @@ DV_API int dv_masked_intersect(int batch_size, int max_n, float xyzmin, float xy
                         int* max_count, void* stream);
 
 /* Count-only pass of dv_masked_intersect. */
+/* last_step (optional, int [batch]): the walk step (1-based) at which each ray
+ * meets its last occupied voxel, 0 if none.  Given to the segment writers as
+ * stop_step (optional), it lets their walk end there instead of at the far
+ * side of the grid (same segments; nothing occupied lies beyond). */
 DV_API int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float voxel_size,
                     float mask_scale, const float* o, const float* v, const uint8_t* mask,
-                    int* intersect_num, int* max_count, void* stream);
+                    int* intersect_num, int* max_count, int* last_step, void* stream);
 
 /*
  * Compacted (CSR) segment lists, the form DIVeR.extract_features builds with
@@ -112,7 +116,7 @@ DV_API int dv_masked_count(int batch_size, float xyzmin, float voxel_num, float 
 DV_API int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
                        float mask_scale, const float* o, const float* v, const uint8_t* mask,
                        const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
-                       void* stream);
+                       const int* stop_step, void* stream);
 DV_API int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, float voxel_size,
                       const float* o, const float* v, const int64_t* offsets, float* seg,
                       float* seg_t, int* seg_ray, void* stream);
@@ -127,11 +131,11 @@ DV_API int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, floa
  */
 DV_API int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size,
                                 const float* o, const float* v, const uint8_t* mask, int* intersect_num,
-                                int* max_count, void* stream);
+                                int* max_count, int* last_step, void* stream);
 DV_API int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size,
                                    const float* o, const float* v, const uint8_t* mask,
                                    const int64_t* offsets, float* seg, float* seg_t, int* seg_ray,
-                                   void* stream);
+                                   const int* stop_step, void* stream);
 
 /* Per-ray segment counts for the dense pairing: max(intersect_num - 1, 0). */
 DV_API int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* seg_count, void* stream);

@@ -51,7 +51,7 @@ def test_argument_errors_need_no_gpu():
     lib = _native.lib()
     # negative sizes and NULL buffers are rejected before any CUDA call
     assert lib.dv_ray_voxel_count(-1, 0.0, 64.0, 1.0, None, None, None, None, None) == 1
-    assert lib.dv_masked_count(8, 0.0, 64.0, 1.0, 1.0, None, None, None, None, None, None) == 1
+    assert lib.dv_masked_count(8, 0.0, 64.0, 1.0, 1.0, None, None, None, None, None, None, None) == 1
     assert lib.dv_aabb_intersect(8, None, None, None, None, None, None, 100, None) == 1
     # empty batches are a no-op success
     assert lib.dv_ray_march(0, None, None, None, None, 64, None) == 0
