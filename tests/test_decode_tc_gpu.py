@@ -201,7 +201,7 @@ def _oracle_rgb_alpha(sc, o, v, xyzmin, n, vs):
 ERR_BOUNDS = {"fp32": 1e-5, "bf16": 1e-3, "fp16": 2e-4}
 
 
-@pytest.mark.parametrize("scene", ["small", "grid256"])
+@pytest.mark.parametrize("scene", ["small", "grid256", "grid256x64"])
 def test_render_error_metrics_vs_fp64(scene):
     from diver_gb300 import scenes
     from diver_gb300.renderer import DIVeRField
@@ -210,10 +210,15 @@ def test_render_error_metrics_vs_fp64(scene):
         sc = scenes.small_scene("cpu")
         o, v = scenes.small_view("cpu")
     else:
-        sc = scenes.grid_scene(256, 32, "diver32", device="cpu")
-        cam = scenes.sphere_cameras(100, 4.0, 3)[0]
+        # grid256: the differentiation scene (DIVeR32, 32 channels); grid256x64: the precision
+        # scene (64-channel features, DIVeR64) on a spiral camera
+        wide = scene == "grid256x64"
+        sc = scenes.grid_scene(256, 64, "diver64", device="cpu") if wide else scenes.grid_scene(256, 32, "diver32",
+                                                                                                device="cpu")
+        cam = scenes.spiral_cameras(200, 4.0)[37] if wide else scenes.sphere_cameras(100, 4.0, 3)[0]
         o, v = scenes.camera_rays(cam, 800, 800, 960.0, "cpu")
-        pick = torch.arange(0, o.shape[0], 313)[:2048]  # a fixed spread-out subset of the frame
+        n = 1024 if wide else 2048
+        pick = torch.arange(0, o.shape[0], 313)[:n]  # a fixed spread-out subset of the frame
         o, v = o[pick].contiguous(), v[pick].contiguous()
     sc.decoder.layers[sc.decoder.n_mlp1 - 1][1][0] += 0.6  # density above zero: a visible, semi-opaque scene
     ref_rgb, ref_alpha = _oracle_rgb_alpha(sc, o, v, sc.xyzmin, sc.voxel_num, sc.voxel_size)
