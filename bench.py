@@ -70,7 +70,7 @@ OUR_LAUNCHES_PER_STEP = 10  # count, 3 x scan, segments, ray_pe, decode_fwd(_tc)
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--frames", type=int, default=8)
@@ -137,7 +137,7 @@ def allreduce_sum(x: float, world: int) -> float:
 
 
 class Clocks:
-    """nvidia-smi samples (every 200 ms) during the timed region."""
+    """nvidia-smi samples (every 50 ms) during the timed region."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -150,8 +150,14 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                          "-lms", "50", "-i", str(self.index)], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
+            # wait for the sampler's first line (taken before the region, not kept) so that the
+            # samples that follow all fall inside the timed region
+            import select
+
+            if select.select([self.proc.stdout], [], [], 5.0)[0]:
+                self.proc.stdout.readline()
         except Exception:
             self.proc = None
         return self
