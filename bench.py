@@ -465,10 +465,16 @@ def run_wide_train(args, dev):
         if keep.numel() >= B:
             keep = keep[:B]
             batches.append((o[keep].contiguous(), d[keep].contiguous(), torch.rand(B, 3, generator=g, device=dev)))
-    out = {"grid": list(sc.dims), "occupancy": float(sc.mask.float().mean()), "batch": B}
+    from diver_gb300.graphs import TrainStepGraph
+
+    out = {"grid": list(sc.dims), "occupancy": float(sc.mask.float().mean()), "batch": B,
+           "form": "the step captured in a CUDA graph (eager in `eager_ms_per_step`)"}
     for form in ("fp32", "bf16"):
-        ms = _time_steps(lambda i: train_step(field, *batches[i % 8], form=form), 2, 8)
-        out[form] = {"ms_per_step": ms, "Mrays_per_s": B / (ms * 1e-3) / 1e6}
+        eager = _time_steps(lambda i: train_step(field, *batches[i % 8], form=form), 2, 8)
+        step = TrainStepGraph(field, *batches[0], form=form, l_s=L_S)
+        ms = _time_steps(lambda i: step(*batches[i % 8]), 3, 16)
+        del step
+        out[form] = {"ms_per_step": ms, "Mrays_per_s": B / (ms * 1e-3) / 1e6, "eager_ms_per_step": eager}
     out["bf16_speedup_vs_fp32"] = out["bf16"]["Mrays_per_s"] / out["fp32"]["Mrays_per_s"]
     return out
 
