@@ -183,8 +183,10 @@ __global__ void __launch_bounds__(128) mlp_eval_kernel(const RtArgs a) {
   float* sw = smem;
   float* rows = smem + L::size;
   stage_weights<W, FIRST>(a.params, sw);
-  float* X = rows + threadIdx.x * (W + 4);               // integrated feature / h2
-  float* H = rows + (blockDim.x + threadIdx.x) * (W + 4);  // h1
+  // one row per thread serves as the input of every layer: each layer's output
+  // is in registers before the row is rewritten (integrated feature, h1, h2)
+  float* X = rows + threadIdx.x * (W + 4);
+  float* H = X;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.batch || a.finish[b]) return;
   float pe[PE_PAD];
@@ -300,9 +302,9 @@ __global__ void __launch_bounds__(128) rt_frame_kernel(const RtFrameArgs a) {
   float* sw = smem;
   float* rows = smem + L::size;
   stage_weights<W, FIRST>(a.params, sw);
-  float* X = rows + threadIdx.x * (W + 4);
-  float* H = rows + (blockDim.x + threadIdx.x) * (W + 4);
-  float* hit_slots = rows + 2 * blockDim.x * (W + 4) + threadIdx.x * 48;
+  float* X = rows + threadIdx.x * (W + 4);  // one row for every layer's input (see mlp_eval_kernel)
+  float* H = X;
+  float* hit_slots = rows + blockDim.x * (W + 4) + threadIdx.x * 48;
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.batch) return;
   float4 acc = make_float4(0.f, 0.f, 0.f, 1.f);
@@ -322,7 +324,7 @@ __global__ void __launch_bounds__(128) rt_frame_kernel(const RtFrameArgs a) {
 template <int W, int FIRST>
 int launch_mlp_eval(const RtArgs& a, cudaStream_t st) {
   using L = RtLayout<W, FIRST>;
-  const size_t smem = (size_t)(L::size + 2 * 128 * (W + 4)) * sizeof(float);
+  const size_t smem = (size_t)(L::size + 128 * (W + 4)) * sizeof(float);
   auto k = mlp_eval_kernel<W, FIRST>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
   k<<<ceil_div(a.batch, 128), 128, smem, st>>>(a);
@@ -333,7 +335,7 @@ int launch_mlp_eval(const RtArgs& a, cudaStream_t st) {
 template <int W, int FIRST>
 int launch_rt_frame(const RtFrameArgs& a, cudaStream_t st) {
   using L = RtLayout<W, FIRST>;
-  const size_t smem = (size_t)(L::size + 2 * 128 * (W + 4) + 128 * 48) * sizeof(float);
+  const size_t smem = (size_t)(L::size + 128 * (W + 4) + 128 * 48) * sizeof(float);
   auto k = rt_frame_kernel<W, FIRST>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
   k<<<ceil_div(a.batch, 128), 128, smem, st>>>(a);
