@@ -228,10 +228,11 @@ def test_camera_rays_on_device_match_reference_math():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n_rays", [3000, 60000])
+@pytest.mark.parametrize("n_rays", [3000, 40001, 60000])
 def test_masked_segments_both_writers_bit_exact(n_rays):
     """Small batches write segments per lane, large ones stage them per warp
-    (masked_emit_staged_kernel): both give the oracle's CSR lists bit for bit."""
+    (masked_emit_staged_kernel, also with a partly filled last warp): both
+    give the oracle's CSR lists bit for bit."""
     from diver_gb300 import masked_segments, scenes
 
     sc = scenes.small_scene("cpu")
