@@ -29,6 +29,8 @@ SIGNATURES = {
     "dv_masked_intersect": (I32, [I32, I32, F32, F32, F32, F32, F32, P, P, P, P, P, P, P, P]),
     "dv_masked_count": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P, P]),
     "dv_masked_segments": (I32, [I32, F32, F32, F32, F32, P, P, P, P, P, P, P, P, P]),
+    "dv_masked_segments_slots": (I32, [I32, F32, F32, F32, F32, P, P, P, I64, P, P, P, P, P]),
+    "dv_compact_slots": (I32, [I32, I64, P, P, P, P, P, P, P]),
     "dv_masked_count_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P]),
     "dv_masked_segments_grid": (I32, [I32, P, P, F32, P, P, P, P, P, P, P, P, P]),
     "dv_dense_segments": (I32, [I32, F32, F32, F32, P, P, P, P, P, P, P]),

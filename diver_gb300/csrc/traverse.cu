@@ -14,7 +14,9 @@
 
 namespace dv {
 
-enum WalkMode { WALK_COUNT = 0, WALK_PADDED = 1, WALK_SEGMENTS = 2 };
+// WALK_SLOTS: one walk both counts and writes, each ray into its own fixed
+// range of `slot` rows (b * slot ...), compacted into CSR lists afterwards.
+enum WalkMode { WALK_COUNT = 0, WALK_PADDED = 1, WALK_SEGMENTS = 2, WALK_SLOTS = 3 };
 
 struct WalkArgs {
   int batch;
@@ -38,6 +40,7 @@ struct WalkArgs {
   int* max_count;
   int* last_step;          // count: per ray, the walk step (1-based) of its last occupied voxel, 0 if none
   const int* stop_step;    // segments: per ray, the step after which the walk may stop (last_step of the count)
+  long long slot;          // slots: rows per ray
   const int64_t* offsets;
   float* seg;
   float* seg_t;
@@ -217,6 +220,10 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
     base = a.offsets[b];
     cap = a.offsets[b + 1] - base;
   }
+  if (MODE == WALK_SLOTS) {
+    base = (int64_t)b * a.slot;
+    cap = a.slot;
+  }
   SegWriter w;
   int count = 0;
   bool done = false;
@@ -268,14 +275,14 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
           rr[5] = P[k + 1].z;
           trow[count] = __fmul_rn(T[k], a.voxel_size);
         }
-        if (MODE == WALK_SEGMENTS && count < cap)
+        if ((MODE == WALK_SEGMENTS || MODE == WALK_SLOTS) && count < cap)
           w.put(a, b, base + count, count + 1 < cap, P[k], P[k + 1], __fmul_rn(T[k], a.voxel_size));
         ++count;
       }
     }
     p = P[LOOKAHEAD];  // only read again when all LOOKAHEAD steps stayed inside
   }
-  if (MODE == WALK_SEGMENTS) w.flush(a, b);
+  if (MODE == WALK_SEGMENTS || MODE == WALK_SLOTS) w.flush(a, b);
   if (MODE == WALK_COUNT && a.last_step) a.last_step[b] = last;
   return count;
 }
@@ -418,6 +425,26 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
     nb = 0;
     __syncwarp();
   }
+}
+
+// Slots -> CSR: row k of ray b moves from b * slot + k to offsets[b] + k.
+__global__ void __launch_bounds__(256) compact_slots_kernel(int batch, long long slot, const int64_t* __restrict__ offsets,
+                                                            const float* __restrict__ sseg,
+                                                            const float* __restrict__ st, float* __restrict__ seg,
+                                                            float* __restrict__ t, int* __restrict__ ray) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long b = i / slot, k = i - b * slot;
+  if (b >= batch) return;
+  const long long beg = offsets[b];
+  if (k >= offsets[b + 1] - beg) return;
+  const long long src = i, dst = beg + k;
+  const float2* s2 = reinterpret_cast<const float2*>(sseg + src * 6);
+  float2* d2 = reinterpret_cast<float2*>(seg + dst * 6);
+  d2[0] = s2[0];
+  d2[1] = s2[1];
+  d2[2] = s2[2];
+  if (t) t[dst] = st[src];
+  if (ray) ray[dst] = (int)b;
 }
 
 // Octree first hit.  Reference ray_march.cu:33-148, generalised from the
@@ -799,6 +826,37 @@ int dv_masked_segments(int batch_size, float xyzmin, float voxel_num, float voxe
     masked_emit_staged_kernel<<<ceil_div(batch_size, STAGE_THREADS), STAGE_THREADS, 0, (cudaStream_t)stream>>>(a);
   else
     DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_masked_segments_slots(int batch_size, float xyzmin, float voxel_num, float voxel_size, float mask_scale,
+                             const float* o, const float* v, const uint8_t* mask, long long slot, float* seg_slots,
+                             float* t_slots, int* intersect_num, int* max_count, void* stream) {
+  DV_CHECK(batch_size >= 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(o && v && mask && seg_slots && t_slots && intersect_num, DV_ERR_ARG);
+  DV_CHECK(slot >= (long long)(3.0f * voxel_num) + 3, DV_ERR_ARG);  // no ray crosses more planes
+  DV_CHECK(segment_buffers_aligned(seg_slots, t_slots, nullptr, 16), DV_ERR_ARG);
+  WalkArgs a = walk_args(batch_size, xyzmin, voxel_num, voxel_size, mask_scale, o, v, mask);
+  a.slot = slot;
+  a.seg = seg_slots;
+  a.seg_t = t_slots;
+  a.num = intersect_num;
+  a.max_count = max_count;
+  DV_WALK_LAUNCH(masked_walk_kernel<WALK_SLOTS>, batch_size, stream, a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_compact_slots(int batch_size, long long slot, const int64_t* offsets, const float* seg_slots,
+                     const float* t_slots, float* seg, float* seg_t, int* seg_ray, void* stream) {
+  DV_CHECK(batch_size >= 0 && slot > 0, DV_ERR_ARG);
+  if (batch_size == 0) return DV_OK;
+  DV_CHECK(offsets && seg_slots && t_slots && seg, DV_ERR_ARG);
+  DV_CHECK(aligned_to(seg_slots, 8) && aligned_to(seg, 8), DV_ERR_ARG);
+  compact_slots_kernel<<<ceil_div((long long)batch_size * slot, 256), 256, 0, (cudaStream_t)stream>>>(
+      batch_size, slot, offsets, seg_slots, t_slots, seg, seg_t, seg_ray);
   DV_TRY_LAUNCH();
   return DV_OK;
 }

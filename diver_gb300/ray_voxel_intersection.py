@@ -187,6 +187,21 @@ def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capac
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
+    if capacity is not None and B > 0:
+        # fixed capacity: one walk writes every ray into its own range of rows
+        # (slots), then the slots are compacted into the CSR lists
+        S = _capacity(capacity, B, 3 * int(voxel_num))
+        slot = 3 * int(voxel_num) + 3
+        mx = torch.zeros(1, dtype=torch.int32, device=dev)
+        sseg = torch.empty(B * slot, 6, dtype=torch.float32, device=dev)
+        st_ = torch.empty(B * slot, dtype=torch.float32, device=dev)
+        N.call("dv_masked_segments_slots", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+               N.ptr(o), N.ptr(v), N.ptr(m8), slot, N.ptr(sseg), N.ptr(st_), N.ptr(num), N.ptr(mx), st)
+        offsets = exclusive_scan(num)
+        seg, t, ray = _buffers(S, dev)
+        N.call("dv_compact_slots", B, slot, N.ptr(offsets), N.ptr(sseg), N.ptr(st_), N.ptr(seg), N.ptr(t), N.ptr(ray),
+               st)
+        return Segments(offsets, seg, t, ray, num, None, mx)
     last = torch.empty(B, dtype=torch.int32, device=dev)  # where each ray's emission walk may stop
     mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),

@@ -129,6 +129,19 @@ DV_API int dv_dense_segments(int batch_size, float xyzmin, float voxel_num, floa
  * bytes.  With equal values on the three axes the arithmetic is exactly that
  * of dv_masked_count / dv_masked_segments (mask_scale 1).
  */
+/* One walk instead of count + segments, for callers with fixed-capacity
+ * buffers: ray b writes its segments (seg, t as dv_masked_segments) into rows
+ * b * slot ... of seg_slots [batch * slot][6] / t_slots and its count into
+ * intersect_num (max into max_count, optional); slot >= 3 * voxel_num + 3
+ * (no ray crosses more grid planes).  Then dv_exclusive_scan of the counts and
+ * dv_compact_slots give the CSR lists (seg, seg_t, seg_ray). */
+DV_API int dv_masked_segments_slots(int batch_size, float xyzmin, float voxel_num, float voxel_size,
+                                    float mask_scale, const float* o, const float* v, const uint8_t* mask,
+                                    long long slot, float* seg_slots, float* t_slots, int* intersect_num,
+                                    int* max_count, void* stream);
+DV_API int dv_compact_slots(int batch_size, long long slot, const int64_t* offsets, const float* seg_slots,
+                            const float* t_slots, float* seg, float* seg_t, int* seg_ray, void* stream);
+
 DV_API int dv_masked_count_grid(int batch_size, const float* xyzmin, const int* dims, float voxel_size,
                                 const float* o, const float* v, const uint8_t* mask, int* intersect_num,
                                 int* max_count, int* last_step, void* stream);
