@@ -43,6 +43,8 @@ SIGNATURES = {
     "dv_integrate_fwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_integrate_bwd": (I32, [P, I32, I32, I32, I32, P, P, I64, I64, P, P]),
     "dv_corner_rows": (I32, [P, P, I64, I64, I32, P, P]),
+    "dv_mark_corner_rows": (I32, [P, I64, P, I32, I32, I32, P, P]),
+    "dv_clear_marked_rows": (I32, [P, I32, I32, I32, I32, P, P]),
     "dv_integrate_table_fwd": (I32, [P, I64, I32, P, P, P, I64, I64, P, P]),
     "dv_integrate_table_bwd": (I32, [P, I64, I32, P, P, P, I64, I64, P, P]),
     "dv_decoder_param_count": (I32, [I32, I32]),

@@ -122,6 +122,63 @@ static int check_common(const IntegrateArgs& a) {
   return DV_OK;
 }
 
+// ---- clearing only the gradient rows a step wrote ------------------------
+//
+// A training step accumulates into the 8 corner rows of each of its segments,
+// a small part of a large grid (about 3 M of 17 M rows for 4096 rays through a
+// 256^3 grid), so zeroing the whole gradient before every step moves ~5x the
+// bytes the step writes.  mark_rows_kernel sets one byte per segment at its
+// lower corner; clear_rows_kernel zeroes every row that is a corner of a
+// marked cell (rows r with a mark at r - {0,1}^3), a warp writing its 32
+// consecutive rows as contiguous float4 runs.
+
+__global__ void __launch_bounds__(256) mark_rows_kernel(const float* __restrict__ seg, long long cap,
+                                                        const int64_t* __restrict__ n_dev, int nvx, int nvy, int nvz,
+                                                        uint8_t* __restrict__ touched) {
+  const long long n = segment_total(cap, n_dev);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < n; s += stride) {
+    const float* p = seg + 6 * s;
+    const SegCorner c = segment_corners(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3), __ldg(p + 4),
+                                        __ldg(p + 5), nvx, nvy, nvz);
+    touched[((long long)c.z * nvy + c.y) * nvx + c.x] = 1;
+  }
+}
+
+template <int F4>  // float4 per row; 0: runtime f4
+__global__ void __launch_bounds__(256) clear_rows_kernel(float4* __restrict__ grid, int f4, int nvx, int nvy, int nvz,
+                                                         const uint8_t* __restrict__ touched) {
+  const int per_row = F4 ? F4 : f4;
+  const long long rows = (long long)nvx * nvy * nvz;
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  // w is the same for every lane of a warp, so the loop and the ballot are warp-uniform
+  for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w * 32 < rows; w += warps) {
+    const long long r = w * 32 + lane;
+    bool dirty = false;
+    if (r < rows) {
+      const int x = (int)(r % nvx);
+      const long long zy = r / nvx;
+      const int y = (int)(zy % nvy), z = (int)(zy / nvy);
+#pragma unroll
+      for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 2; ++dx) {
+            const int zz = z - dz, yy = y - dy, xx = x - dx;
+            if (zz >= 0 && yy >= 0 && xx >= 0)
+              dirty |= __ldg(touched + ((long long)zz * nvy + yy) * nvx + xx) != 0;
+          }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, dirty);
+    if (m == 0) continue;
+    float4* base = grid + w * 32 * per_row;
+    for (int e = lane; e < 32 * per_row; e += 32)
+      if ((m >> (e / per_row)) & 1u) base[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
 }  // namespace dv
 
 using namespace dv;
@@ -227,6 +284,38 @@ int dv_integrate_table_bwd(const float* grad_feature, long long n_rows, int chan
   a.C = channels;
   integrate_table_bwd_kernel<<<ceil_div(n_seg * (channels / 4), 256), 256, 0, (cudaStream_t)stream>>>(a);
   DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_mark_corner_rows(const float* seg, long long n_seg, const int64_t* n_seg_dev, int nvx, int nvy, int nvz,
+                        uint8_t* touched, void* stream) {
+  DV_CHECK(n_seg >= 0 && nvx > 0 && nvy > 0 && nvz > 0, DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(seg && touched, DV_ERR_ARG);
+  const unsigned need = ceil_div(n_seg, 256);
+  const unsigned blocks = need < 152u * 8u ? need : 152u * 8u;
+  mark_rows_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(seg, n_seg, n_seg_dev, nvx, nvy, nvz, touched);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_clear_marked_rows(float* grid, int channels, int nvx, int nvy, int nvz, uint8_t* touched, void* stream) {
+  DV_CHECK(channels > 0 && (channels & 3) == 0 && nvx > 0 && nvy > 0 && nvz > 0, DV_ERR_ARG);
+  DV_CHECK(grid && touched && ((uintptr_t)grid & 15) == 0, DV_ERR_ARG);
+  const long long rows = (long long)nvx * nvy * nvz;
+  const unsigned need = ceil_div(rows, 256);
+  const unsigned blocks = need < 152u * 8u ? need : 152u * 8u;
+  float4* g = reinterpret_cast<float4*>(grid);
+  const cudaStream_t st = (cudaStream_t)stream;
+  const int f4 = channels / 4;
+  if (f4 == 8)
+    clear_rows_kernel<8><<<blocks, 256, 0, st>>>(g, f4, nvx, nvy, nvz, touched);
+  else if (f4 == 16)
+    clear_rows_kernel<16><<<blocks, 256, 0, st>>>(g, f4, nvx, nvy, nvz, touched);
+  else
+    clear_rows_kernel<0><<<blocks, 256, 0, st>>>(g, f4, nvx, nvy, nvz, touched);
+  DV_TRY_LAUNCH();
+  if (cudaMemsetAsync(touched, 0, (size_t)rows, st) != cudaSuccess) return DV_ERR_CUDA;
   return DV_OK;
 }
 

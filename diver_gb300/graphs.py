@@ -15,8 +15,13 @@ gradients, is recorded once in a CUDA graph and replayed.
 
 Inputs are copied into the graph's own buffers before each replay; outputs
 are the graph's buffers (overwritten by the next replay; clone to keep them).
-The grid gradient's zero fill (2.2 GB for a 256^3 x 32 grid) is issued on a
-second stream at the start of the step, and the backward waits for it.
+The grid gradient is zeroed on a second stream at the start of the step, and
+the backward waits for that.  By default only the rows the previous replay
+wrote are zeroed (dv_clear_marked_rows; the backward marks its segments'
+corner cells with dv_mark_corner_rows): about a fifth of a 256^3 x 32 grid's
+2.2 GB for a 4096-ray batch.  The returned grid gradient must then be treated
+as read-only between replays (clone it to change it); sparse_clear=False
+zero-fills the whole buffer every step instead.
 The tensor-core weight images are repacked from the parameters inside the
 graph, so optimizer steps between replays are seen by the next replay.
 """
@@ -24,7 +29,8 @@ from __future__ import annotations
 
 import torch
 
-from .renderer import DIVeRField
+from . import _native as N
+from .renderer import DIVeRField, _grid
 
 
 def _warm_and_capture(fn, warmup: int):
@@ -45,11 +51,15 @@ class TrainStepGraph:
     example (o [B,3], d [B,3], target [B,3])."""
 
     def __init__(self, field: DIVeRField, o: torch.Tensor, d: torch.Tensor, target: torch.Tensor,
-                 form: str = "bf16", l_s: float = 1e-5, warmup: int = 2):
+                 form: str = "bf16", l_s: float = 1e-5, warmup: int = 2, sparse_clear: bool = True):
         self.field, self.form, self.l_s = field, form, float(l_s)
         self.o, self.d, self.target = o.clone().contiguous(), d.clone().contiguous(), target.clone().contiguous()
         self.capacity = field.segment_capacity(o.shape[0])
         self._grid_grad = torch.zeros_like(field.voxels)
+        self._shape = _grid(field.voxels)
+        nx, ny, nz, _ = self._shape
+        # a byte per grid row: the cells whose corners the last replay wrote
+        self._touched = torch.zeros(nz * ny * nx, dtype=torch.uint8, device=o.device) if sparse_clear else None
         self._fill = torch.cuda.Stream(o.device)
         field.refresh_always = True
         try:
@@ -62,10 +72,16 @@ class TrainStepGraph:
         main = torch.cuda.current_stream()
         self._fill.wait_stream(main)  # the previous step's use of the buffer is done
         with torch.cuda.stream(self._fill):
-            self._grid_grad.zero_()
+            if self._touched is None:
+                self._grid_grad.zero_()
+            else:
+                nx, ny, nz, c = self._shape
+                N.call("dv_clear_marked_rows", N.ptr(self._grid_grad), c, nx, ny, nz, N.ptr(self._touched),
+                       N.stream(self._grid_grad.device))
             filled = torch.cuda.Event()
             filled.record()
-        rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity, grad_voxels=(self._grid_grad, filled))
+        rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity,
+                     grad_voxels=(self._grid_grad, filled, self._touched))
         loss = torch.nn.functional.mse_loss(rgb, self.target) + self.l_s * reg
         gv, gp = torch.autograd.grad(loss, [f.voxels, f.params])
         return loss.detach(), gv, gp

@@ -188,10 +188,14 @@ class SegmentRender(Function):
         _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb),
                1.0 / B if scale is not None else 0.0, N.ptr(scale), N.ptr(d4), st)
         if ctx.grad_voxels is not None:
-            # caller-owned buffer, zero-filled on another stream while the
-            # forward ran; wait for that fill
-            gv, filled = ctx.grad_voxels
+            # caller-owned buffer, zeroed on another stream while the forward
+            # ran; wait for that, then mark the rows this step writes when the
+            # caller clears only those (dv_clear_marked_rows)
+            gv, filled, *touched = ctx.grad_voxels
             torch.cuda.current_stream(dev).wait_event(filled)
+            if touched and touched[0] is not None:
+                N.call("dv_mark_corner_rows", N.ptr(seg.seg), seg.total, seg.count_ptr, nx, ny, nz, N.ptr(touched[0]),
+                       st)
         else:
             gv = torch.zeros_like(voxels)
         gp = torch.zeros_like(params)
@@ -210,7 +214,9 @@ def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_b
     grid the tensor-core forward reads its corner rows from.  grad_voxels
     (training, optional): (buffer, event) — a grid-shaped buffer that is all
     zeros once `event` has completed; the grid gradient is accumulated into it
-    and returned as it, so its zero fill can overlap the forward."""
+    and returned as it, so its zero fill can overlap the forward.  A third
+    element, a uint8 byte per grid row, has the backward mark the rows it
+    writes (dv_mark_corner_rows) for the caller's next dv_clear_marked_rows."""
     # whether a backward will follow is known here, not inside the Function's
     # forward (which always runs with grad mode off): only then does the
     # tensor-core forward keep its layer tiles for the backward

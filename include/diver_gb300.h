@@ -340,6 +340,21 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
                             long long saved_bytes, const float* out4, float* grad_voxels,
                             float* grad_params, int* err, void* stream);
 
+/* Clearing a grid gradient where a step wrote it (no counterpart in the
+ * reference, whose optimizer zeroes the whole dense gradient every step).
+ * touched: a byte per grid row (nvz * nvy * nvx, zero-initialised).
+ * dv_mark_corner_rows sets the byte of the lower corner (as the integration
+ * computes it) of each of the n_seg segments seg [n_seg][6] (n_seg_dev, when
+ * not null, a device count <= n_seg of the valid ones).  dv_clear_marked_rows
+ * zeroes every row of grid [nvz][nvy][nvx][channels] that is one of the 8
+ * corners of a marked cell, then zeroes touched.  Marking a step's segments
+ * after clearing and before its gradient scatter keeps the buffer zero
+ * everywhere the next step does not write. */
+DV_API int dv_mark_corner_rows(const float* seg, long long n_seg, const int64_t* n_seg_dev, int nvx,
+                               int nvy, int nvz, uint8_t* touched, void* stream);
+DV_API int dv_clear_marked_rows(float* grid, int channels, int nvx, int nvy, int nvz, uint8_t* touched,
+                                void* stream);
+
 /* Pinhole camera rays of pixels [first_pixel, first_pixel + n_pixels) of an
  * H x W image, row-major (utils/dataset/ray_utils.py:5-55): rays_o / rays_d
  * [n_pixels][3] (device); c2w is a HOST float [3][4] camera-to-world matrix;

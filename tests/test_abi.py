@@ -80,6 +80,12 @@ def test_argument_errors_of_the_later_entry_points_need_no_gpu():
     assert lib.dv_camera_rays(4, 4, 1.0, (C.c_float * 12)(), 10, 10, fake, fake, None) == 1  # past the image
     assert lib.dv_realtime_frame(32, 8, fake, fake, fake, 100, fake, fake, fake, 101, fake, fake, None) == 1  # N % 64
     assert lib.dv_realtime_frame(48, 8, fake, fake, fake, 64, fake, fake, fake, 65, fake, fake, None) == 1  # width
+    assert lib.dv_mark_corner_rows(None, 0, None, 33, 33, 33, None, None) == 0
+    assert lib.dv_mark_corner_rows(fake, 10, None, 0, 33, 33, fake, None) == 1  # empty grid
+    assert lib.dv_mark_corner_rows(fake, 10, None, 33, 33, 33, None, None) == 1  # no byte map
+    assert lib.dv_clear_marked_rows(fake, 30, 33, 33, 33, fake, None) == 1  # channels % 4
+    assert lib.dv_clear_marked_rows(C.c_void_p(20), 32, 33, 33, 33, fake, None) == 1  # grid not 16-byte aligned
+    assert lib.dv_clear_marked_rows(None, 32, 33, 33, 33, fake, None) == 1
     assert lib.dv_decode_tc_save_bytes(32, 32, 128) == 128 * 2 * (32 + 4 * 32)
     assert lib.dv_decode_tc_save_bytes(33, 32, 128) == -1
     # a layer table whose shapes do not fit the blob is rejected
