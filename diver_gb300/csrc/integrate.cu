@@ -129,8 +129,9 @@ static int check_common(const IntegrateArgs& a) {
 // 256^3 grid), so zeroing the whole gradient before every step moves ~5x the
 // bytes the step writes.  mark_rows_kernel sets one byte per segment at its
 // lower corner; clear_rows_kernel zeroes every row that is a corner of a
-// marked cell (rows r with a mark at r - {0,1}^3), a warp writing its 32
-// consecutive rows as contiguous float4 runs.
+// marked cell (rows r with a mark at r - {0,1}^3): a warp walks one (z, y)
+// line of rows 32 at a time and writes the dirty ones of each 32 as
+// contiguous float4 runs.
 
 __global__ void __launch_bounds__(256) mark_rows_kernel(const float* __restrict__ seg, long long cap,
                                                         const int64_t* __restrict__ n_dev, int nvx, int nvy, int nvz,
@@ -149,33 +150,37 @@ template <int F4>  // float4 per row; 0: runtime f4
 __global__ void __launch_bounds__(256) clear_rows_kernel(float4* __restrict__ grid, int f4, int nvx, int nvy, int nvz,
                                                          const uint8_t* __restrict__ touched) {
   const int per_row = F4 ? F4 : f4;
-  const long long rows = (long long)nvx * nvy * nvz;
+  const int lines = nvy * nvz;  // rows of one (z, y) are contiguous in x
   const int lane = threadIdx.x & 31;
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  // w is the same for every lane of a warp, so the loop and the ballot are warp-uniform
-  for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w * 32 < rows; w += warps) {
-    const long long r = w * 32 + lane;
-    bool dirty = false;
-    if (r < rows) {
-      const int x = (int)(r % nvx);
-      const long long zy = r / nvx;
-      const int y = (int)(zy % nvy), z = (int)(zy / nvy);
-#pragma unroll
-      for (int dz = 0; dz < 2; ++dz)
-#pragma unroll
-        for (int dy = 0; dy < 2; ++dy)
-#pragma unroll
-          for (int dx = 0; dx < 2; ++dx) {
-            const int zz = z - dz, yy = y - dy, xx = x - dx;
-            if (zz >= 0 && yy >= 0 && xx >= 0)
-              dirty |= __ldg(touched + ((long long)zz * nvy + yy) * nvx + xx) != 0;
-          }
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  // one warp per line; everything below is warp-uniform except x
+  for (int line = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; line < lines; line += warps) {
+    const int y = line % nvy, z = line / nvy;
+    // the marks of the 4 lines (z - dz, y - dy) whose cells have this line's rows as corners
+    const uint8_t* m00 = touched + (long long)line * nvx;
+    const uint8_t* m01 = y > 0 ? m00 - nvx : nullptr;
+    const uint8_t* m10 = z > 0 ? m00 - (long long)nvy * nvx : nullptr;
+    const uint8_t* m11 = (y > 0 && z > 0) ? m10 - nvx : nullptr;
+    float4* base = grid + (long long)line * nvx * per_row;
+    unsigned carry = 0;  // the OR of the 4 marks at x - 1 for lane 0 (previous chunk's lane 31)
+    for (int x0 = 0; x0 < nvx; x0 += 32) {
+      const int x = x0 + lane;
+      unsigned u = 0;
+      if (x < nvx) {
+        u = __ldg(m00 + x);
+        if (m01) u |= __ldg(m01 + x);
+        if (m10) u |= __ldg(m10 + x);
+        if (m11) u |= __ldg(m11 + x);
+      }
+      const unsigned left = __shfl_up_sync(0xffffffffu, u, 1);
+      const bool dirty = x < nvx && (u | (lane ? left : carry)) != 0;
+      carry = __shfl_sync(0xffffffffu, u, 31);
+      const unsigned m = __ballot_sync(0xffffffffu, dirty);
+      if (m == 0) continue;
+      float4* b = base + (long long)x0 * per_row;
+      for (int e = lane; e < 32 * per_row; e += 32)
+        if ((m >> (e / per_row)) & 1u) b[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    const unsigned m = __ballot_sync(0xffffffffu, dirty);
-    if (m == 0) continue;
-    float4* base = grid + w * 32 * per_row;
-    for (int e = lane; e < 32 * per_row; e += 32)
-      if ((m >> (e / per_row)) & 1u) base[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
@@ -302,9 +307,13 @@ int dv_mark_corner_rows(const float* seg, long long n_seg, const int64_t* n_seg_
 int dv_clear_marked_rows(float* grid, int channels, int nvx, int nvy, int nvz, uint8_t* touched, void* stream) {
   DV_CHECK(channels > 0 && (channels & 3) == 0 && nvx > 0 && nvy > 0 && nvz > 0, DV_ERR_ARG);
   DV_CHECK(grid && touched && ((uintptr_t)grid & 15) == 0, DV_ERR_ARG);
+  DV_CHECK((long long)nvy * nvz < (1ll << 31), DV_ERR_ARG);
   const long long rows = (long long)nvx * nvy * nvz;
-  const unsigned need = ceil_div(rows, 256);
-  const unsigned blocks = need < 152u * 8u ? need : 152u * 8u;
+  // 1 block per SM: the clear runs beside the step's traversal on another
+  // stream, and a grid that filled every SM's thread slots with grid-stride
+  // blocks would keep the traversal's blocks from starting until it ended
+  const unsigned need = ceil_div((long long)nvy * nvz, 8);  // 8 warps (lines) per block
+  const unsigned blocks = need < 152u ? need : 152u;
   float4* g = reinterpret_cast<float4*>(grid);
   const cudaStream_t st = (cudaStream_t)stream;
   const int f4 = channels / 4;
