@@ -135,7 +135,7 @@ class TcWeights:
 class SegmentRender(Function):
     @staticmethod
     def forward(ctx, voxels, params, seg: Segments, dirs, kind: int, white_back: bool, tc: TcWeights | None = None,
-                voxels16: torch.Tensor | None = None, training: bool = False, grad_voxels=None):
+                voxels16: torch.Tensor | None = None, training: bool = False, grad_voxels=None, pe=None):
         nx, ny, nz, c = _grid(voxels)
         _check_params(kind, c, params)
         N.need_cuda("dirs", dirs, torch.float32)
@@ -143,9 +143,12 @@ class SegmentRender(Function):
         dev = voxels.device
         st = N.stream(dev)
         W = WIDTH[kind]
-        pe_feat = torch.empty(B, 28, device=dev)
-        pe_out = torch.empty(B, W, device=dev)
-        _timed("dv_ray_pe", kind, c, N.ptr(params), B, N.ptr(dirs), N.ptr(pe_feat), N.ptr(pe_out), st)
+        if pe is None:
+            pe_feat = torch.empty(B, 28, device=dev)
+            pe_out = torch.empty(B, W, device=dev)
+            _timed("dv_ray_pe", kind, c, N.ptr(params), B, N.ptr(dirs), N.ptr(pe_feat), N.ptr(pe_out), st)
+        else:
+            pe_feat, pe_out = pe
         S = seg.total
         out4 = torch.empty(S, 4, device=dev)
         if tc is None:
@@ -201,14 +204,14 @@ class SegmentRender(Function):
         gp = torch.zeros_like(params)
         if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st,
                                                   getattr(ctx, "saved_layers", None), out4):
-            return gv, gp, None, None, None, None, None, None, None, None
+            return gv, gp, None, None, None, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
-        return gv, gp, None, None, None, None, None, None, None, None
+        return gv, gp, None, None, None, None, None, None, None, None, None
 
 
 def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None,
-                    voxels16: torch.Tensor | None = None, grad_voxels=None):
+                    voxels16: torch.Tensor | None = None, grad_voxels=None, pe=None):
     """(rgb [B,3], sparsity term) for the CSR segments of B rays.  `tc` selects
     the tensor-core decoder; `voxels16` (inference) is a BF16/FP16 copy of the
     grid the tensor-core forward reads its corner rows from.  grad_voxels
@@ -216,13 +219,15 @@ def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_b
     zeros once `event` has completed; the grid gradient is accumulated into it
     and returned as it, so its zero fill can overlap the forward.  A third
     element, a uint8 byte per grid row, has the backward mark the rows it
-    writes (dv_mark_corner_rows) for the caller's next dv_clear_marked_rows."""
+    writes (dv_mark_corner_rows) for the caller's next dv_clear_marked_rows.
+    pe (optional): (pe_feat [B,28], pe_out [B,W]) of dv_ray_pe for these
+    directions and parameters, when the caller computed them already."""
     # whether a backward will follow is known here, not inside the Function's
     # forward (which always runs with grad mode off): only then does the
     # tensor-core forward keep its layer tiles for the backward
     training = torch.is_grad_enabled() and (voxels.requires_grad or params.requires_grad)
     return SegmentRender.apply(voxels, params, seg, dirs, KIND_ID.get(kind, kind), white_back, tc, voxels16, training,
-                               grad_voxels)
+                               grad_voxels, pe)
 
 
 class DIVeRField(torch.nn.Module):
@@ -331,7 +336,32 @@ class DIVeRField(torch.nn.Module):
         autograd the tensor-core forms read a 16-bit copy of the grid.
         capacity: fixed segment buffers, no host synchronisation (see segments).
         grad_voxels: see render_segments."""
-        seg = self.segments(os.contiguous(), ds.contiguous(), capacity)
+        os, ds = os.contiguous(), ds.contiguous()
+        N.need_cuda("dirs", ds, torch.float32)
+        dev = self.voxels.device
+        kind = KIND_ID[self.kind]
+        # the tensor-core weight images and the directions' encoding do not
+        # depend on the segments: they run on a side stream beside the
+        # traversal, which occupies one warp per SM (the outputs are
+        # allocated on the calling stream, which waits for the side stream)
+        main = torch.cuda.current_stream(dev)
+        side = self._side_stream(dev)
+        pe = (torch.empty(ds.shape[0], 28, device=dev), torch.empty(ds.shape[0], WIDTH[kind], device=dev))
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            tc = self.tc_weights(form)
+            if ds.shape[0]:
+                _check_params(kind, self.voxels.shape[-1], self.params)
+                _timed("dv_ray_pe", kind, self.voxels.shape[-1], N.ptr(self.params), ds.shape[0], N.ptr(ds),
+                       N.ptr(pe[0]), N.ptr(pe[1]), N.stream(dev))
+        seg = self.segments(os, ds, capacity)
+        main.wait_stream(side)
         g16 = self.grid16(form) if not torch.is_grad_enabled() else None
-        return render_segments(self.voxels, self.params, seg, ds.contiguous(), self.kind, self.white_back,
-                               self.tc_weights(form), g16, grad_voxels)
+        return render_segments(self.voxels, self.params, seg, ds, self.kind, self.white_back, tc, g16, grad_voxels,
+                               pe)
+
+    def _side_stream(self, dev) -> torch.cuda.Stream:
+        s = getattr(self, "_side", None)
+        if s is None or s.device != dev:
+            s = self._side = torch.cuda.Stream(dev)
+        return s
