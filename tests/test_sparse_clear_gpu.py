@@ -70,6 +70,29 @@ def test_clear_zeroes_exactly_the_written_rows(channels, shape):
     assert int(touched.sum().item()) == 0
 
 
+def test_clear_of_long_lines():
+    """Lines of 800 rows (25 chunks of 32 rows; the x - 1 neighbour's mark
+    carried from chunk to chunk); random segments."""
+    nz, ny, nx, channels = 4, 5, 800, 32
+    g = torch.Generator().manual_seed(3)
+    p0 = torch.rand(500, 3, generator=g) * torch.tensor([nx - 1.0, ny - 1.0, nz - 1.0])
+    p1 = (p0 + torch.rand(500, 3, generator=g) * 0.9).clamp_max(torch.tensor([nx - 1.0, ny - 1.0, nz - 1.0]))
+    seg = torch.cat([p0, p1], 1).float().cuda().contiguous()
+    grid = torch.randn(nz, ny, nx, channels, device="cuda") + 5.0
+    before = grid.clone()
+    touched = torch.zeros(nz * ny * nx, dtype=torch.uint8, device="cuda")
+    st = N.stream(grid.device)
+    N.call("dv_mark_corner_rows", N.ptr(seg), seg.shape[0], None, nx, ny, nz, N.ptr(touched), st)
+    N.call("dv_clear_marked_rows", N.ptr(grid), channels, nx, ny, nz, N.ptr(touched), st)
+    torch.cuda.synchronize()
+    expect = torch.zeros(nz * ny * nx, dtype=torch.bool)
+    expect[corner_rows(seg, nx, ny, nz).reshape(-1)] = True
+    flat, ref = grid.reshape(-1, channels).cpu(), before.reshape(-1, channels).cpu()
+    assert torch.equal((flat == 0).all(1), expect)
+    assert torch.equal(flat[~expect], ref[~expect])
+    assert int(touched.sum().item()) == 0
+
+
 def test_mark_stops_at_the_device_count():
     nz = ny = nx = 33
     segs = walk_segments(32, 200, 7)
