@@ -18,6 +18,7 @@ on bounded samples of the same workload.
 from __future__ import annotations
 
 import argparse
+import math
 import json
 import os
 import statistics
@@ -317,17 +318,30 @@ def run_ours(args, rank, world, local):
         train_forms["speedup_vs_fp32"] = {m: train_forms[tform][m]["Mrays_per_s"] / train_forms["fp32"][m]["Mrays_per_s"]
                                           for m in ("eager", "graph")}
     # ---- e2e: pinned host inputs, H2D + D2H inside the timed region ----
+    # a training loop's pattern: each step's loss is copied to a pinned host
+    # slot and read on the host while the next step runs (one step in flight)
     host = [tuple(t.cpu().pin_memory() for t in b) for b in batches[args.warmup:]]
+    loss_host = [torch.empty(1, pin_memory=True) for _ in range(2)]
+    copied = [torch.cuda.Event() for _ in range(2)]
+    losses = []
     torch.cuda.synchronize()
     barrier(world)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record()
-    for o_h, d_h, g_h in host:
+    for i, (o_h, d_h, g_h) in enumerate(host):
         loss, _, _ = step(o_h, d_h, g_h)  # H2D copies into the graph's inputs, replay
-        loss.item()
+        loss_host[i % 2].copy_(loss.reshape(1), non_blocking=True)
+        copied[i % 2].record()
+        if i > 0:
+            copied[(i - 1) % 2].synchronize()
+            losses.append(loss_host[(i - 1) % 2].item())
+    copied[(len(host) - 1) % 2].synchronize()
+    losses.append(loss_host[(len(host) - 1) % 2].item())
     t1.record()
     torch.cuda.synchronize()
+    if len(losses) != len(host) or not all(math.isfinite(x) for x in losses):
+        raise RuntimeError("end-to-end training loop produced a non-finite or missing loss")
     e2e_ms = allreduce_max(t0.elapsed_time(t1), world)
     e2e_val = rays / (e2e_ms * 1e-3) / 1e6
     # ---- render: full frames, forward only, per decoder form ----
