@@ -57,6 +57,11 @@ SIGNATURES = {
     "dv_decode_fwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, I64, P,
                                P]),
     "dv_decode_tc_save_bytes": (I64, [I32, I32, I64]),
+    "dv_decode_fwd_tc_split": (I32, [I32, I32, P, I32, P, I32, P, I32, P, I32, I32, I32, P, P, I64, P, P, P, P, I64,
+                                     P, P]),
+    "dv_decode_tc_split_save_bytes": (I64, [I32, I32, I64]),
+    "dv_decode_bwd_tc_split": (I32, [I32, I32, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P, P, P, I64, P, P, P,
+                                     P, P]),
     "dv_wait_selftest": (I32, [I32, P, P]),
     "dv_decode_bwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, P, I32, P, I32, P, I32, I32, I32, P, P, I64, P, P,
                                P, P, P, I64, P, P, P, P, P]),

@@ -44,7 +44,7 @@ struct TcArgs {
   const float* pe_out;  // [B][W]: bias + PE part of mlp2's first layer (FP32)
   float4* out4;
   const uint8_t* wblob;
-  int wbytes;  // multiple of 16
+  int wbytes;  // bytes of one term's weight images (multiple of 16); TERMS terms follow each other
   const float* bias;
   int nbias;   // multiple of 4
   TcLayer L[TC_MAX_LAYERS];
@@ -54,8 +54,12 @@ struct TcArgs {
   int save_bytes;      // bytes per tile record (sum of 256 * K over the layers)
 };
 
-template <int C, int BF16>
-__device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, long long s0, uint8_t* sA) {
+// Gather from the FP32 grid: C/4 threads per segment, each integrating 4
+// channels; the feature row goes to the A tile as TERMS operand terms (tile
+// term i at sA + i * tstride).
+template <int C, int BF16, int TERMS>
+__device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, long long s0, uint8_t* sA,
+                                               uint32_t tstride) {
   constexpr int TPS = C / 4;
   constexpr int SPP = 128 / TPS;
   const int t = threadIdx.x;
@@ -71,8 +75,16 @@ __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, lon
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
       f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
     }
-    uint2 v = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
-    *reinterpret_cast<uint2*>(sA + tc::kmajor_offset(ls, 4 * q, C)) = v;
+    uint8_t* dst = sA + tc::kmajor_offset(ls, 4 * q, C);
+    if constexpr (TERMS == 1) {
+      *reinterpret_cast<uint2*>(dst) = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
+    } else {
+      uint32_t x[TERMS], y[TERMS];
+      tc::split_pair<TERMS>(f.x, f.y, x);
+      tc::split_pair<TERMS>(f.z, f.w, y);
+#pragma unroll
+      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint2*>(dst + i * tstride) = make_uint2(x[i], y[i]);
+    }
   }
 }
 
@@ -130,24 +142,36 @@ __device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long S, lon
 }
 
 // Issues one layer's MMA chain (thread 0) and waits for it (all threads).
-// With `save`, thread 0 also copies the layer's input tile (the A operand,
-// 256 * K bytes) to global memory by a bulk async copy and, before the
-// caller's barrier lets anyone overwrite A, waits until that copy has read it.
-template <int BF16>
-__device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, const uint8_t* sA, uint32_t tmem,
-                                         uint64_t* bar, uint32_t& phase, uint8_t* save = nullptr) {
+// With TERMS = 3 the A tile and the weight images are three BF16 terms each
+// and the chain sums the six products whose term indices add up to at most 2
+// (FP32-grade products).  With `save`, thread 0 also copies the layer's input
+// tile (the A operand, 256 * K bytes; with TERMS = 3 its first two terms, a
+// two-term split of the same values) to global memory by bulk async copies
+// and, before the caller's barrier lets anyone overwrite A, waits until those
+// copies have read it.
+template <int BF16, int TERMS>
+__device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, uint32_t wterm, const uint8_t* sA,
+                                         uint32_t tstride, uint32_t tmem, uint64_t* bar, uint32_t& phase,
+                                         uint8_t* save = nullptr) {
+  constexpr int NP = TERMS == 1 ? 1 : 6;
+  constexpr int PA[6] = {0, 0, 1, 0, 2, 1};  // term of A, per product
+  constexpr int PB[6] = {0, 1, 0, 2, 0, 1};  // term of B
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
     if (save != nullptr) {
       tc::bulk_store(save, sA, (uint32_t)L.K * 256u);
+      if (TERMS > 1) tc::bulk_store(save + L.K * 256, sA + tstride, (uint32_t)L.K * 256u);
       tc::bulk_commit();
     }
     const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
-    const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB + L.b_off);
     const uint32_t sbo = (uint32_t)(L.K / 8) * 128;
-    for (int k = 0; k < L.K / 16; ++k)
-      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
-                  k > 0 ? 1u : 0u);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      const uint32_t a0 = tc::smem_u32(sA + PA[p] * tstride), b0 = tc::smem_u32(sB + PB[p] * wterm + L.b_off);
+      for (int k = 0; k < L.K / 16; ++k)
+        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
+                    (p > 0 || k > 0) ? 1u : 0u);
+    }
     tc::mma_commit(bar);
   }
   const bool done = tc::mbar_wait_bounded(bar, phase);
@@ -157,17 +181,29 @@ __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, co
   return done;
 }
 
-// Writes 32 values (columns c0..c0+31 of the next layer's input) of row t.
-template <int BF16>
-__device__ __forceinline__ void store_row32(uint8_t* sA, int t, int c0, int K, const float* v) {
+// Writes 32 values (columns c0..c0+31 of the next layer's input) of row t,
+// as TERMS operand terms (term i at sA + i * tstride).
+template <int BF16, int TERMS>
+__device__ __forceinline__ void store_row32(uint8_t* sA, uint32_t tstride, int t, int c0, int K, const float* v) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    uint4 w;
-    w.x = tc::pack2<BF16>(v[8 * j + 0], v[8 * j + 1]);
-    w.y = tc::pack2<BF16>(v[8 * j + 2], v[8 * j + 3]);
-    w.z = tc::pack2<BF16>(v[8 * j + 4], v[8 * j + 5]);
-    w.w = tc::pack2<BF16>(v[8 * j + 6], v[8 * j + 7]);
-    *reinterpret_cast<uint4*>(sA + tc::kmajor_offset(t, c0 + 8 * j, K)) = w;
+    uint8_t* dst = sA + tc::kmajor_offset(t, c0 + 8 * j, K);
+    if constexpr (TERMS == 1) {
+      uint4 w;
+      w.x = tc::pack2<BF16>(v[8 * j + 0], v[8 * j + 1]);
+      w.y = tc::pack2<BF16>(v[8 * j + 2], v[8 * j + 3]);
+      w.z = tc::pack2<BF16>(v[8 * j + 4], v[8 * j + 5]);
+      w.w = tc::pack2<BF16>(v[8 * j + 6], v[8 * j + 7]);
+      *reinterpret_cast<uint4*>(dst) = w;
+    } else {
+      uint32_t x[TERMS], y[TERMS], z[TERMS], u[TERMS];
+      tc::split_pair<TERMS>(v[8 * j + 0], v[8 * j + 1], x);
+      tc::split_pair<TERMS>(v[8 * j + 2], v[8 * j + 3], y);
+      tc::split_pair<TERMS>(v[8 * j + 4], v[8 * j + 5], z);
+      tc::split_pair<TERMS>(v[8 * j + 6], v[8 * j + 7], u);
+#pragma unroll
+      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint4*>(dst + i * tstride) = make_uint4(x[i], y[i], z[i], u[i]);
+    }
   }
 }
 
@@ -177,18 +213,21 @@ __device__ __forceinline__ void sync_for_mma() {
   __syncthreads();
 }
 
-// NCOLS: TMEM columns (>= widest N, power of two >= 32).
-template <int C, int W, int D1, int BF16, int NCOLS>
+// NCOLS: TMEM columns (>= widest N, power of two >= 32).  TERMS: operand
+// terms (1: BF16 or FP16 operands; 3: FP32 values as three BF16 terms, six
+// products per layer, FP32-grade; BF16 only and read from the FP32 grid).
+template <int C, int W, int D1, int BF16, int NCOLS, int TERMS>
 __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
   constexpr int KMAX = C > W ? C : W;
+  constexpr uint32_t TSTRIDE = 128 * KMAX * 2;  // bytes between the A tile's terms
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* sB = smem;
-  float* sBias = reinterpret_cast<float*>(smem + a.wbytes);
+  float* sBias = reinterpret_cast<float*>(smem + TERMS * a.wbytes);
   uint8_t* sA = reinterpret_cast<uint8_t*>(sBias + a.nbias);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sA + 128 * KMAX * 2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sA + TERMS * TSTRIDE);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   const int t = threadIdx.x, warp = t >> 5;
-  for (int i = t; i < a.wbytes / 16; i += 128)
+  for (int i = t; i < TERMS * a.wbytes / 16; i += 128)
     reinterpret_cast<uint4*>(sB)[i] = __ldg(reinterpret_cast<const uint4*>(a.wblob) + i);
   for (int i = t; i < a.nbias; i += 128) sBias[i] = __ldg(a.bias + i);
   if (t == 0) {
@@ -203,6 +242,7 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
   const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lanes
+  const uint32_t wterm = (uint32_t)a.wbytes;
   uint32_t phase = 0;
   bool ok = true;
   const long long S = segment_total(a.S, a.S_dev);
@@ -213,16 +253,16 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     const bool valid = s < S;
     uint8_t* rec = a.save ? a.save + tile * (long long)a.save_bytes : nullptr;
 #define DV_SAVE(l) (rec ? rec + a.save_off[l] : nullptr)
-    if (a.grid16)
+    if (TERMS == 1 && a.grid16)
       gather_tile_16<C, BF16>(a, S, s0, sA);
     else
-      gather_tile_lp<C, BF16>(a, S, s0, sA);
+      gather_tile_lp<C, BF16, TERMS>(a, S, s0, sA, TSTRIDE);
     sync_for_mma();
     float v[32];
     // mlp1 hidden layers: D = relu(A W^T + b)
 #pragma unroll 1
     for (int l = 0; l < D1 && ok; ++l) {
-      ok = tc_layer<BF16>(a.L[l], sB, sA, tmem, bar, phase, DV_SAVE(l));
+      ok = tc_layer<BF16, TERMS>(a.L[l], sB, wterm, sA, TSTRIDE, tmem, bar, phase, DV_SAVE(l));
       ok = __syncthreads_and(ok);
       if (!ok) break;
 #pragma unroll
@@ -231,13 +271,13 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
         tc::ld_wait();
 #pragma unroll
         for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + sBias[a.L[l].bias_off + c0 + i], 0.f);
-        store_row32<BF16>(sA, t, c0, W, v);
+        store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
       }
       sync_for_mma();
     }
     if (!ok) break;
     // mlp1 output: columns 0..W-1 hidden (no activation), column W sigma
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1], sB, sA, tmem, bar, phase, DV_SAVE(D1)));
+    ok = __syncthreads_and(tc_layer<BF16, TERMS>(a.L[D1], sB, wterm, sA, TSTRIDE, tmem, bar, phase, DV_SAVE(D1)));
     if (!ok) break;
     float sigma;
     {
@@ -252,11 +292,12 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
       tc::ld_wait();
 #pragma unroll
       for (int i = 0; i < 32; ++i) v[i] += sBias[a.L[D1].bias_off + c0 + i];
-      store_row32<BF16>(sA, t, c0, W, v);
+      store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
     }
     sync_for_mma();
     // mlp2 first layer: relu(hidden W^T + per-ray (bias + PE term))
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 1], sB, sA, tmem, bar, phase, DV_SAVE(D1 + 1)));
+    ok = __syncthreads_and(
+        tc_layer<BF16, TERMS>(a.L[D1 + 1], sB, wterm, sA, TSTRIDE, tmem, bar, phase, DV_SAVE(D1 + 1)));
     if (!ok) break;
     {
       const int ray = valid ? __ldg(a.seg_ray + s) : 0;
@@ -273,12 +314,13 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
           v[i + 2] = fmaxf(v[i + 2] + p.z, 0.f);
           v[i + 3] = fmaxf(v[i + 3] + p.w, 0.f);
         }
-        store_row32<BF16>(sA, t, c0, W, v);
+        store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
       }
     }
     sync_for_mma();
     // mlp2 output: 3 logits -> sigmoid
-    ok = __syncthreads_and(tc_layer<BF16>(a.L[D1 + 2], sB, sA, tmem, bar, phase, DV_SAVE(D1 + 2)));
+    ok = __syncthreads_and(
+        tc_layer<BF16, TERMS>(a.L[D1 + 2], sB, wterm, sA, TSTRIDE, tmem, bar, phase, DV_SAVE(D1 + 2)));
 #undef DV_SAVE
     if (!ok) break;
     {
@@ -304,12 +346,12 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
 // The persistent grid holds as many CTAs per SM as registers, shared memory
 // and TMEM (512 columns) allow together (the occupancy API under-reports
 // kernels that allocate TMEM).
-template <int C, int W, int D1, int BF16>
+template <int C, int W, int D1, int BF16, int TERMS = 1>
 int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
   constexpr int NCOLS = W == 32 ? 64 : 128;
   constexpr int KMAX = C > W ? C : W;
-  const size_t smem = (size_t)a.wbytes + (size_t)a.nbias * 4 + 128 * KMAX * 2 + 16;
-  auto k = decode_fwd_tc<C, W, D1, BF16, NCOLS>;
+  const size_t smem = (size_t)TERMS * a.wbytes + (size_t)a.nbias * 4 + (size_t)TERMS * 128 * KMAX * 2 + 16;
+  auto k = decode_fwd_tc<C, W, D1, BF16, NCOLS, TERMS>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return DV_ERR_CUDA;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -348,23 +390,21 @@ __global__ void wait_selftest_kernel(uint32_t limit, int* status) {
 
 using namespace dv;
 
-extern "C" {
-
-int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
-                     const int* layers, int n_layers, const float* voxels, const void* voxels16, int nvx, int nvy,
-                     int nvz, const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
-                     const float* pe_out, float* out4, void* save, long long save_capacity, int* err,
-                     void* stream) {
-  DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
+// Checks the arguments of a tensor-core forward launch and fills TcArgs;
+// terms: operand terms (1, or 3 for the split-operand form; the save record
+// then holds two terms of every layer input).
+static int decode_fwd_tc_args(TcArgs& a, int kind, int channels, int terms, const void* wblob, int wbytes,
+                              const float* bias, int nbias, const int* layers, int n_layers, const float* voxels,
+                              const void* voxels16, int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
+                              long long n_seg, const int64_t* n_seg_dev, const float* pe_out, float* out4, void* save,
+                              long long save_capacity, int* err) {
   const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
   DV_CHECK(d1 > 0 && n_layers == d1 + 3 && n_layers <= TC_MAX_LAYERS, DV_ERR_ARG);
   DV_CHECK((kind == 32 && channels == 32) || (kind == 64 && (channels == 32 || channels == 64)), DV_ERR_UNSUPPORTED);
-  if (n_seg == 0) return DV_OK;
   DV_CHECK(wblob && bias && layers && voxels && seg && seg_ray && pe_out && out4, DV_ERR_ARG);
   DV_CHECK(wbytes > 0 && wbytes % 16 == 0 && nbias > 0 && nbias % 4 == 0, DV_ERR_ARG);
   DV_CHECK(((uintptr_t)wblob & 15) == 0 && ((uintptr_t)voxels & 15) == 0 && ((uintptr_t)out4 & 15) == 0, DV_ERR_ARG);
   DV_CHECK(voxels16 == nullptr || ((uintptr_t)voxels16 & 15) == 0, DV_ERR_ARG);
-  TcArgs a{};
   a.grid = voxels;
   a.grid16 = reinterpret_cast<const uint16_t*>(voxels16);
   a.nvx = nvx;
@@ -393,12 +433,13 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
     DV_CHECK((long long)L.b_off + (long long)L.N * L.K * 2 <= wbytes && L.bias_off + L.N <= nbias, DV_ERR_ARG);
     DV_CHECK(L.N <= (W == 32 ? 64 : 128), DV_ERR_ARG);
   }
-  // saved layer inputs: one record of sum(256 K) bytes per 128-segment tile
+  // saved layer inputs: one record of sum(256 K) bytes (per saved term) per 128-segment tile
   if (save != nullptr) {
+    const int saved_terms = terms > 1 ? 2 : 1;
     int off = 0;
     for (int l = 0; l < n_layers; ++l) {
       a.save_off[l] = off;
-      off += 256 * a.L[l].K;
+      off += 256 * a.L[l].K * saved_terms;
     }
     a.save = reinterpret_cast<uint8_t*>(save);
     a.save_bytes = off;
@@ -410,11 +451,53 @@ int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wb
   for (int l = 1; l < d1; ++l) DV_CHECK(a.L[l].K == W && a.L[l].N == W, DV_ERR_ARG);
   DV_CHECK(a.L[d1].K == W && a.L[d1].N >= W + 4, DV_ERR_ARG);
   DV_CHECK(a.L[d1 + 1].K == W && a.L[d1 + 1].N == W && a.L[d1 + 2].K == W && a.L[d1 + 2].N >= 16, DV_ERR_ARG);
+  return DV_OK;
+}
+
+extern "C" {
+
+int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
+                     const int* layers, int n_layers, const float* voxels, const void* voxels16, int nvx, int nvy,
+                     int nvz, const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                     const float* pe_out, float* out4, void* save, long long save_capacity, int* err,
+                     void* stream) {
+  DV_CHECK(n_seg >= 0 && (bf16 == 0 || bf16 == 1), DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  TcArgs a{};
+  const int rc = decode_fwd_tc_args(a, kind, channels, 1, wblob, wbytes, bias, nbias, layers, n_layers, voxels,
+                                    voxels16, nvx, nvy, nvz, seg, seg_ray, n_seg, n_seg_dev, pe_out, out4, save,
+                                    save_capacity, err);
+  if (rc != DV_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind == 32) return bf16 ? launch_decode_fwd_tc<32, 32, 2, 1>(a, st) : launch_decode_fwd_tc<32, 32, 2, 0>(a, st);
   if (channels == 32)
     return bf16 ? launch_decode_fwd_tc<32, 64, 1, 1>(a, st) : launch_decode_fwd_tc<32, 64, 1, 0>(a, st);
   return bf16 ? launch_decode_fwd_tc<64, 64, 1, 1>(a, st) : launch_decode_fwd_tc<64, 64, 1, 0>(a, st);
+}
+
+int dv_decode_fwd_tc_split(int kind, int channels, const void* wblob, int wbytes, const float* bias, int nbias,
+                           const int* layers, int n_layers, const float* voxels, int nvx, int nvy, int nvz,
+                           const float* seg, const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                           const float* pe_out, float* out4, void* save, long long save_capacity, int* err,
+                           void* stream) {
+  DV_CHECK(n_seg >= 0, DV_ERR_ARG);
+  if (n_seg == 0) return DV_OK;
+  TcArgs a{};
+  const int rc = decode_fwd_tc_args(a, kind, channels, 3, wblob, wbytes, bias, nbias, layers, n_layers, voxels,
+                                    nullptr, nvx, nvy, nvz, seg, seg_ray, n_seg, n_seg_dev, pe_out, out4, save,
+                                    save_capacity, err);
+  if (rc != DV_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 32) return launch_decode_fwd_tc<32, 32, 2, 1, 3>(a, st);
+  if (channels == 32) return launch_decode_fwd_tc<32, 64, 1, 1, 3>(a, st);
+  return launch_decode_fwd_tc<64, 64, 1, 1, 3>(a, st);
+}
+
+long long dv_decode_tc_split_save_bytes(int kind, int channels, long long n_seg) {
+  const int d1 = kind == 32 ? 2 : (kind == 64 ? 1 : -1);
+  if (d1 < 0 || n_seg < 0) return -1;
+  const long long record = 2 * 256LL * (channels + (d1 + 2) * kind);
+  return (n_seg + 127) / 128 * record;
 }
 
 int dv_wait_selftest(int limit, int* status, void* stream) {

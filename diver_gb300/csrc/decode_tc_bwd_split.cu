@@ -1,0 +1,433 @@
+// Tensor-core (tcgen05) backward of the DIVeR32 decoder with split BF16
+// operands: FP32-grade gradients from BF16 tensor cores.
+//
+// Every FP32 operand is carried as a sum of BF16 terms (tc::split_pair):
+//   - delta propagation  dL/d input = delta @ W: delta and W as three terms
+//     each, the six products whose term indices add up to at most 2;
+//   - weight gradient    dW += delta^T @ activation: two terms each, three
+//     products (FP32 accumulators resident in TMEM for the CTA's life);
+//   - bias gradient      column sums of the two-term delta (CUDA cores).
+// Products are accumulated in FP32 in TMEM, so the propagated deltas and the
+// gradients keep about 2^-24 (propagation) and 2^-16 (weight gradients) of
+// relative precision per product; emulating the kernel's arithmetic on the
+// CPU gives gradients within a few 1e-7 (grid) and 1e-6 (weights) relative
+// of an FP64 backward, where a single BF16 term gives 1e-2.
+//
+// The forward is not recomputed: dv_decode_fwd_tc_split saved, per tile of 128
+// segments, every layer's input as two BF16 terms (X0, A1, A2, hidden, A4;
+// 16 KiB each), and its FP32 out4 gives the colour logits' sigmoid.  The
+// record is read into shared memory by bulk async copies.
+//
+// One CTA = 256 threads over one tile of 128 segments: thread t owns segment
+// row r = t % 128 (TMEM lane r; warps w and w + 4 share a lane quadrant) and
+// half h = t / 128 of each row's columns in the epilogues.  Shared memory
+// (about 162 KiB, one CTA per SM): transposed weight images in three terms,
+// the saved record, the PE tile in two terms, and the delta tile in three
+// terms (48 columns: the widest propagation K).  The weight-gradient MMA reads
+// the delta tile transposed with M = 128 output rows; rows past a layer's
+// outputs read the neighbouring (finite) data of the tile and of the next
+// term and land in TMEM rows that are never read.
+// Reference semantics: the autograd backward of model/diver.py:159-180.
+#include "common.cuh"
+#include "integrate.cuh"
+#include "mlp.cuh"
+#include "tc.cuh"
+
+#include <algorithm>
+
+namespace dv {
+namespace bws {
+
+constexpr int C = 32, W = 32;
+constexpr int NL = 5;
+constexpr int THREADS = 256;
+constexpr int FD = 48;              // delta tile columns (K of the widest propagation MMA)
+constexpr int TILE = 128 * 32 * 2;  // one term of a [128][32] BF16 tile
+constexpr int DTILE = 128 * FD * 2; // one term of the delta tile
+constexpr int TMEM_COLS = 256;
+// layer: 0 (C->W), 1 (W->W), 2 (W->W+1: sigma, hidden), 3 (W+27->W), 4 (W->3)
+__host__ __device__ constexpr int IN(int l) { return l == 0 ? C : (l == 3 ? W + PE_DIM : W); }
+__host__ __device__ constexpr int OUT(int l) { return l == 2 ? W + 1 : (l == 4 ? 3 : W); }
+__host__ __device__ constexpr int OUT4(int l) { return pad4(OUT(l)); }
+__host__ __device__ constexpr int NIN(int l) { return l == 3 ? 64 : 32; }  // weight-gradient columns (in, padded)
+__host__ __device__ constexpr int DWCOL(int l) { return l == 0 ? 64 : (l <= 3 ? DWCOL(l - 1) + NIN(l - 1) : 224); }
+__host__ __device__ constexpr int KPROP(int l) { return l == 4 ? 16 : (l == 2 ? W + 16 : W); }  // propagation K
+constexpr uint32_t RECORD = 5 * 2 * TILE;  // saved record of one tile: 5 layer inputs x 2 terms
+
+struct Args {
+  int nvx, nvy, nvz;
+  const float* seg;
+  const int* seg_ray;
+  long long S;           // segment count, or capacity when S_dev is set
+  const int64_t* S_dev;  // optional device-held count (clamped to S)
+  const float* pe_feat;  // [B][28]
+  const float4* d4;      // [S] (dL/dsigma, dL/drgb)
+  const float4* out4;    // [S] (sigma, sigmoid rgb) of the forward
+  const uint8_t* saved;  // RECORD bytes per tile
+  float* grad_grid;
+  float* grad_params;    // packed torch layout
+  int w_off[NL], b_off[NL];
+  const uint8_t* wb;     // transposed weight images, three terms of wterm bytes
+  int wterm;
+  int b_img[NL];         // byte offset of layer l's image inside a term
+  int* err;
+};
+
+// Shared-memory layout (byte offsets; wterm = 10240 for DIVeR32).
+struct Layout {
+  uint32_t bb, rec, pe, d, bar;
+  __host__ __device__ static Layout make(int wterm) {
+    Layout L;
+    L.bb = 0;
+    L.rec = (uint32_t)(3 * wterm + 1023) / 1024 * 1024;
+    L.pe = L.rec + RECORD;
+    L.d = L.pe + 2 * TILE;
+    L.bar = L.d + 3 * DTILE;
+    return L;
+  }
+  __host__ __device__ uint32_t bytes() const { return bar + 32; }
+};
+
+// Writes n values (multiple of 8) of row r, starting at column c0, as three
+// BF16 terms of a K-major tile with F columns (term i at tile + i * tstride).
+__device__ __forceinline__ void put3(uint8_t* tile, uint32_t tstride, int F, int r, int c0, const float* v, int n) {
+#pragma unroll
+  for (int c = 0; c < n; c += 8) {
+    uint32_t x[3], y[3], z[3], u[3];
+    tc::split_pair<3>(v[c], v[c + 1], x);
+    tc::split_pair<3>(v[c + 2], v[c + 3], y);
+    tc::split_pair<3>(v[c + 4], v[c + 5], z);
+    tc::split_pair<3>(v[c + 6], v[c + 7], u);
+    uint8_t* dst = tile + tc::kmajor_offset(r, c0 + c, F);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) *reinterpret_cast<uint4*>(dst + i * tstride) = make_uint4(x[i], y[i], z[i], u[i]);
+  }
+}
+
+// Same with two terms.
+__device__ __forceinline__ void put2(uint8_t* tile, uint32_t tstride, int F, int r, int c0, const float* v, int n) {
+#pragma unroll
+  for (int c = 0; c < n; c += 8) {
+    uint32_t x[2], y[2], z[2], u[2];
+    tc::split_pair<2>(v[c], v[c + 1], x);
+    tc::split_pair<2>(v[c + 2], v[c + 3], y);
+    tc::split_pair<2>(v[c + 4], v[c + 5], z);
+    tc::split_pair<2>(v[c + 6], v[c + 7], u);
+    uint8_t* dst = tile + tc::kmajor_offset(r, c0 + c, F);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) *reinterpret_cast<uint4*>(dst + i * tstride) = make_uint4(x[i], y[i], z[i], u[i]);
+  }
+}
+
+// Zeroes v[i] where the activation (leading term of a [128][32] tile, row r,
+// columns c0..c0+n-1) is not positive: the ReLU derivative.  The leading
+// BF16 term has the sign of the FP32 activation (and is zero only with it).
+__device__ __forceinline__ void relu_mask(const uint8_t* tile, int r, int c0, float* v, int n) {
+#pragma unroll
+  for (int c = 0; c < n; c += 8) {
+    const uint4 w = *reinterpret_cast<const uint4*>(tile + tc::kmajor_offset(r, c0 + c, 32));
+    const uint32_t x[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (!(tc::bf_lo(x[j]) > 0.f)) v[c + 2 * j] = 0.f;
+      if (!(tc::bf_hi(x[j]) > 0.f)) v[c + 2 * j + 1] = 0.f;
+    }
+  }
+}
+
+// Propagation: TMEM[0..N) = delta [128][K] (three terms, K-major, FD
+// columns) x image^T (image [N][K], three terms of wterm bytes).
+__device__ __forceinline__ void mma_prop(uint32_t tmem, const uint8_t* D, const uint8_t* img, int wterm, int K, int N) {
+  constexpr int PA6[6] = {0, 0, 1, 0, 2, 1};  // term of delta, per product
+  constexpr int PB6[6] = {0, 1, 0, 2, 0, 1};  // term of the weights
+  const uint32_t idesc = tc::idesc_f16(128, N, 1);
+#pragma unroll
+  for (int p = 0; p < 6; ++p) {
+    const uint32_t a0 = tc::smem_u32(D + PA6[p] * DTILE), b0 = tc::smem_u32(img + PB6[p] * wterm);
+    for (int k = 0; k < K / 16; ++k)
+      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, (FD / 8) * 128),
+                  tc::smem_desc(b0 + k * 256, 128, (uint32_t)(K / 8) * 128), idesc, (p > 0 || k > 0) ? 1u : 0u);
+  }
+}
+
+// Weight gradient over the tile's 128 segments: TMEM dW[128 = out][32 = in]
+// += delta^T x act, both MN-major views of row tiles (two terms each; the
+// activation tile [128][32], term stride TILE).
+__device__ __forceinline__ void mma_dw(uint32_t tmem, const uint8_t* D, const uint8_t* act, bool accumulate) {
+  const uint32_t idesc = tc::idesc_f16(128, 32, 1) | (1u << 15) | (1u << 16);
+  constexpr uint32_t lboA = (FD / 8) * 128, lboB = (32 / 8) * 128;
+  constexpr int PA3[3] = {0, 0, 1};  // term of delta, per product
+  constexpr int PB3[3] = {0, 1, 0};  // term of the activation
+#pragma unroll
+  for (int p = 0; p < 3; ++p) {
+    const uint32_t a0 = tc::smem_u32(D + PA3[p] * DTILE), b0 = tc::smem_u32(act + PB3[p] * TILE);
+    for (int k = 0; k < 8; ++k)
+      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 2 * lboA, lboA, 128), tc::smem_desc(b0 + k * 2 * lboB, lboB, 128),
+                  idesc, (accumulate || p > 0 || k > 0) ? 1u : 0u);
+  }
+}
+
+__device__ __forceinline__ void sync_mma() {
+  tc::fence_before_sync();
+  tc::fence_async_smem();
+  __syncthreads();
+}
+
+// Rows [64 h, 64 h + 64) of column c of the two-term delta tile, summed.
+__device__ __forceinline__ float column_sum(const uint8_t* D, int c, int h) {
+  float s = 0.f;
+#pragma unroll 8
+  for (int r = 64 * h; r < 64 * h + 64; ++r) {
+    const uint32_t off = tc::kmajor_offset(r, c, FD);
+    const uint16_t a = *reinterpret_cast<const uint16_t*>(D + off);
+    const uint16_t b = *reinterpret_cast<const uint16_t*>(D + DTILE + off);
+    s += __uint_as_float((uint32_t)a << 16) + __uint_as_float((uint32_t)b << 16);
+  }
+  return s;
+}
+
+__global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const Args a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const Layout lay = Layout::make(a.wterm);
+  uint8_t* Bb = smem + lay.bb;
+  uint8_t* REC = smem + lay.rec;
+  uint8_t* PE = smem + lay.pe;
+  uint8_t* D = smem + lay.d;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.bar);
+  uint64_t* bar_load = bar + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+  float* stage = reinterpret_cast<float*>(REC);  // [128][C + 4] FP32, once the record is consumed
+
+  const int t = threadIdx.x, warp = t >> 5, r = t & 127, h = t >> 7;
+  for (int i = t; i < 3 * a.wterm / 16; i += THREADS)
+    reinterpret_cast<uint4*>(Bb)[i] = __ldg(reinterpret_cast<const uint4*>(a.wb) + i);
+  for (int i = t; i < 3 * DTILE / 16; i += THREADS) reinterpret_cast<uint4*>(D)[i] = make_uint4(0, 0, 0, 0);
+  if (t == 0) {
+    tc::mbar_init(bar, 1);
+    tc::mbar_init(bar_load, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(tslot, TMEM_COLS);
+    tc::tmem_relinquish();
+  }
+  sync_mma();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
+  const uint32_t trow = tmem + lane;
+  uint32_t phase = 0, phase_load = 0;
+  bool ok = true, first = true;
+  float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float v[32];
+
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + 127) / 128;
+  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+    const long long s = tile * 128 + r;
+    const bool valid = s < S;
+    sync_mma();  // the previous tile is done with the record, the staging alias, PE and D
+    if (t == 0) {
+      const uint8_t* rec = a.saved + tile * (long long)RECORD;
+      tc::mbar_arrive_expect_tx(bar_load, RECORD);
+      for (int l = 0; l < NL; ++l) tc::bulk_load(REC + l * 2 * TILE, rec + l * 2 * TILE, 2 * TILE, bar_load);
+    }
+    // PE tile (columns 16h..16h+15 of row r; PE_DIM = 27 values, zeros after)
+    const int ray = valid ? __ldg(a.seg_ray + s) : 0;
+    {
+      const float* pf = a.pe_feat + (long long)ray * PE_PAD + 16 * h;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = (16 * h + i < PE_DIM) ? __ldg(pf + i) : 0.f;
+      put2(PE, TILE, 32, r, 16 * h, v, 16);
+    }
+    // delta of the colour logits: dL/drgb * sigmoid'
+    const float4 g = valid ? a.d4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (h == 0) {
+      const float4 oc = valid ? a.out4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = 0.f;
+      v[0] = g.y * oc.y * (1.f - oc.y);
+      v[1] = g.z * oc.z * (1.f - oc.z);
+      v[2] = g.w * oc.w * (1.f - oc.w);
+      put3(D, DTILE, FD, r, 0, v, 16);
+    }
+    ok = __syncthreads_and(tc::mbar_wait_bounded(bar_load, phase_load));
+    phase_load ^= 1u;
+    if (!ok) break;
+    sync_mma();
+
+    // layers last to first (unrolled: every layer constant is a compile-time value)
+#pragma unroll
+    for (int l = NL - 1; l >= 0; --l) {
+      const uint8_t* act = REC + l * 2 * TILE;  // this layer's input, two terms TILE apart
+      if (t == 0) {
+        tc::fence_after_sync();
+        mma_prop(tmem, D, Bb + a.b_img[l], a.wterm, KPROP(l), l == 0 ? C : W);
+        if (l == 3) {
+          mma_dw(tmem + DWCOL(3), D, act, !first);
+          mma_dw(tmem + DWCOL(3) + 32, D, PE, !first);
+        } else {
+          mma_dw(tmem + DWCOL(l), D, act, !first);
+        }
+        tc::mma_commit(bar);
+      }
+      if (r < OUT(l)) bias_acc[l] += column_sum(D, r, h);
+      const bool done = tc::mbar_wait_bounded(bar, phase);
+      phase ^= 1u;
+      tc::fence_after_sync();
+      ok = __syncthreads_and(done);  // also: every column sum is done before D is rewritten
+      if (!ok) break;
+      if (l == 3) {
+        // delta of layer 2: (dL/dsigma, d hidden[0..31]) in columns 0..32, zeros to 47;
+        // half 0 writes columns 0..23, half 1 columns 24..47
+        tc::ld_32x32b_x32(trow, v);
+        tc::ld_wait();
+        float w[24];
+        if (h == 0) {
+          w[0] = g.x;
+#pragma unroll
+          for (int i = 1; i < 24; ++i) w[i] = v[i - 1];
+        } else {
+#pragma unroll
+          for (int i = 0; i < 24; ++i) w[i] = (i + 23 < W) ? v[i + 23] : 0.f;
+        }
+        put3(D, DTILE, FD, r, 24 * h, w, 24);
+      } else if (l > 0) {
+        tc::ld_32x32b_x16(trow + 16 * h, v);
+        tc::ld_wait();
+        relu_mask(act, r, 16 * h, v, 16);  // this layer's input is relu of the previous layer's output
+        put3(D, DTILE, FD, r, 16 * h, v, 16);
+      } else {
+        // dL/dfeature, FP32, to the staging rows (the record is consumed)
+        tc::ld_32x32b_x16(trow + 16 * h, v);
+        tc::ld_wait();
+        float* st = stage + r * (C + 4) + 16 * h;
+#pragma unroll
+        for (int i = 0; i < 16; i += 4)
+          *reinterpret_cast<float4*>(st + i) =
+              valid ? make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      sync_mma();
+    }
+    if (!ok) break;
+    first = false;
+    // ---- scatter dL/dfeature into the corner rows ----
+    {
+      constexpr int TPS = C / 4;
+#pragma unroll 1
+      for (int i = t; i < 128 * TPS; i += THREADS) {
+        const int ls = i / TPS, q = i % TPS;
+        const long long ss = tile * 128 + ls;
+        if (ss < S) {
+          const float* sg = a.seg + ss * 6;
+          const SegCorner sc = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3),
+                                               __ldg(sg + 4), __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
+          const float4 gf = *reinterpret_cast<const float4*>(stage + ls * (C + 4) + 4 * q);
+          scatter4(a.grad_grid, sc, C, q, gf, a.nvx, a.nvy);
+        }
+      }
+    }
+  }
+  if (!ok && t == 0 && a.err) atomicExch(a.err, 1);
+  // ---- flush: weight gradients from TMEM (row o = out index = this thread's lane) ----
+  if (ok && !first) {
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const int o = r;
+#pragma unroll
+      for (int c0 = 0; c0 < NIN(l); c0 += 32) {
+        tc::ld_32x32b_x16(tmem + lane + DWCOL(l) + c0 + 16 * h, v);
+        tc::ld_wait();
+        if (o < OUT(l)) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int c = c0 + 16 * h + i;
+            if (c < IN(l)) atomicAdd(a.grad_params + a.w_off[l] + c * OUT4(l) + o, v[i]);
+          }
+        }
+      }
+      if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, bias_acc[l]);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_dealloc(tmem, TMEM_COLS);
+}
+
+}  // namespace bws
+}  // namespace dv
+
+using namespace dv;
+
+extern "C" {
+
+int dv_decode_bwd_tc_split(int kind, int channels, const void* wb, int wb_term_bytes, const int* b_layers,
+                           int n_layers, int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
+                           long long n_seg, const int64_t* n_seg_dev, const float* pe_feat, const float* d4,
+                           const void* saved, long long saved_bytes, const float* out4, float* grad_voxels,
+                           float* grad_params, int* err, void* stream) {
+  using namespace dv::bws;
+  DV_CHECK(n_seg >= 0, DV_ERR_ARG);
+  DV_CHECK(kind == 32 && channels == 32 && n_layers == NL, DV_ERR_UNSUPPORTED);
+  if (n_seg == 0) return DV_OK;
+  DV_CHECK(wb && b_layers && seg && seg_ray && pe_feat && d4 && saved && out4 && grad_voxels && grad_params,
+           DV_ERR_ARG);
+  DV_CHECK(nvx > 0 && nvy > 0 && nvz > 0 && wb_term_bytes > 0 && wb_term_bytes % 16 == 0, DV_ERR_ARG);
+  DV_CHECK(((uintptr_t)wb & 15) == 0 && ((uintptr_t)saved & 15) == 0 && ((uintptr_t)out4 & 15) == 0 &&
+               ((uintptr_t)grad_voxels & 15) == 0 && ((uintptr_t)d4 & 15) == 0,
+           DV_ERR_ARG);
+  DV_CHECK((n_seg + 127) / 128 * (long long)RECORD <= saved_bytes, DV_ERR_ARG);
+  Args a{};
+  a.nvx = nvx;
+  a.nvy = nvy;
+  a.nvz = nvz;
+  a.seg = seg;
+  a.seg_ray = seg_ray;
+  a.S = n_seg;
+  a.S_dev = n_seg_dev;
+  a.pe_feat = pe_feat;
+  a.d4 = reinterpret_cast<const float4*>(d4);
+  a.out4 = reinterpret_cast<const float4*>(out4);
+  a.saved = reinterpret_cast<const uint8_t*>(saved);
+  a.grad_grid = grad_voxels;
+  a.grad_params = grad_params;
+  a.wb = reinterpret_cast<const uint8_t*>(wb);
+  a.wterm = wb_term_bytes;
+  a.err = err;
+  // packed torch layout offsets (same rule as dv_decoder_param_count)
+  {
+    int off = 0;
+    const int outs[NL] = {W, W, W + 1, W, 3};
+    for (int l = 0; l < NL; ++l) {
+      a.w_off[l] = off;
+      a.b_off[l] = off + IN(l) * pad4(outs[l]);
+      off = a.b_off[l] + pad4(outs[l]);
+    }
+  }
+  // transposed images [N = in][K = out padded to 16], inside one term
+  const int bK[NL] = {W, W, W + 16, W, 16}, bN[NL] = {C, W, W, W, W};
+  for (int l = 0; l < NL; ++l) {
+    a.b_img[l] = b_layers[3 * l];
+    DV_CHECK(b_layers[3 * l + 1] == bK[l] && b_layers[3 * l + 2] == bN[l] && bK[l] == KPROP(l), DV_ERR_ARG);
+    DV_CHECK(a.b_img[l] % 16 == 0 && a.b_img[l] >= 0, DV_ERR_ARG);
+    DV_CHECK((long long)a.b_img[l] + (long long)bK[l] * bN[l] * 2 <= wb_term_bytes, DV_ERR_ARG);
+  }
+  const Layout lay = Layout::make(wb_term_bytes);
+  const size_t smem = lay.bytes();
+  auto k = decode_bwd_tc_split_kernel;
+  int dev = 0, sms = 0, smem_max = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  DV_CHECK((long long)smem <= (long long)smem_max, DV_ERR_UNSUPPORTED);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DV_ERR_CUDA;
+  const long long tiles = (n_seg + 127) / 128;
+  const long long grid = std::min<long long>(tiles, (long long)sms);
+  k<<<(unsigned)grid, THREADS, smem, (cudaStream_t)stream>>>(a);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+}  // extern "C"

@@ -146,6 +146,18 @@ __device__ __forceinline__ void ld_32x32b_x32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void ld_32x32b_x16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void ld_32x32b_x4(uint32_t taddr, float* v) {
   uint32_t r[4];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
@@ -165,6 +177,29 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
   else
     asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
   return r;
+}
+
+// Low / high BF16 element of a bf16x2 word as a float.
+__device__ __forceinline__ float bf_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+// FP32 pair (a, b) as a sum of TERMS BF16 pairs: w[0] = RN(a, b), then each
+// further term rounds what the previous ones left.  Every residual is exact in
+// FP32 (a minus its value rounded to 8 significant bits keeps only a's low
+// bits), so the terms sum to (a, b) within 2^-8 (one term), 2^-16 (two) or
+// 2^-24 (three) of its magnitude.  A product of two such sums, taken as the
+// BF16 products whose term indices add up to at most TERMS - 1 (1, 3 or 6
+// tensor-core MMAs), keeps that precision: the split-operand ("BF16x3",
+// "BF16x6") emulation of FP32 products on BF16 tensor cores.
+template <int TERMS>
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t* w) {
+  w[0] = pack2<1>(a, b);
+#pragma unroll
+  for (int i = 1; i < TERMS; ++i) {
+    a = __fsub_rn(a, bf_lo(w[i - 1]));
+    b = __fsub_rn(b, bf_hi(w[i - 1]));
+    w[i] = pack2<1>(a, b);
+  }
 }
 
 // Residency of a persistent kernel whose CTAs each allocate `ncols` TMEM

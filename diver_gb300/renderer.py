@@ -60,63 +60,103 @@ def _check_params(kind: int, channels: int, params: torch.Tensor):
         raise ValueError(f"packed decoder must hold {n} floats, got {params.numel()}")
 
 
-class TcWeights:
-    """Decoder weights in the tensor-core operand layout (BF16 or FP16) on the
-    device.  The images are gathered from the packed plain parameters on the
-    device (`refresh`), into buffers that keep their addresses, so a refresh
-    after an optimizer step needs no host round trip and can sit inside a
-    captured CUDA graph."""
+# Decoder forms: 'fp32' (plain FP32 kernels), 'bf16' / 'fp16' (tensor-core
+# decoder with 16-bit operands: the render form; a 16-bit copy of the grid
+# without autograd), 'bf16s' (tensor-core decoder with split BF16 operands:
+# FP32-grade products from BF16 tensor cores, the accurate training form).
+FORMS = ("fp32", "bf16", "fp16", "bf16s")
 
-    def __init__(self, kind: str, channels: int, device, bf16: bool = True):
+
+def split_terms(x: torch.Tensor, n: int) -> list[torch.Tensor]:
+    """FP32 values as n BF16 terms (each rounds what the previous ones left;
+    every residual is exact in FP32): their sum is x within 2^-(8n) of |x|."""
+    out, r = [], x.float()
+    for _ in range(n):
+        t = r.to(torch.bfloat16)
+        out.append(t)
+        r = r - t.float()
+    return out
+
+
+class TcWeights:
+    """Decoder weights in the tensor-core operand layout on the device.  The
+    images are gathered from the packed plain parameters on the device
+    (`refresh`), into buffers that keep their addresses, so a refresh after an
+    optimizer step needs no host round trip and can sit inside a captured CUDA
+    graph.  mode: 'bf16', 'fp16', or 'bf16s' (every image as three BF16 terms,
+    one after the other, for the split-operand kernels)."""
+
+    def __init__(self, kind: str, channels: int, device, bf16: bool = True, mode: str | None = None):
+        mode = mode or ("bf16" if bf16 else "fp16")
+        if mode not in ("bf16", "fp16", "bf16s"):
+            raise ValueError(f"unknown tensor-core form {mode!r}")
         maps = tc_index_maps(kind, channels)
-        self.kind, self.channels, self.bf16 = kind, channels, bool(bf16)
-        self.dtype = torch.bfloat16 if bf16 else torch.float16
+        self.kind, self.channels, self.mode = kind, channels, mode
+        self.bf16 = mode != "fp16"
+        self.terms = 3 if mode == "bf16s" else 1
+        self.dtype = torch.float16 if mode == "fp16" else torch.bfloat16
         self._i_fwd = maps["fwd"].to(device)
         self._i_bias = maps["bias"].to(device)
         self.table = maps["table"].contiguous()
-        self.blob = torch.zeros(self._i_fwd.numel() * 2, dtype=torch.uint8, device=device)
+        self.term_bytes = self._i_fwd.numel() * 2
+        self.blob = torch.zeros(self.terms * self.term_bytes, dtype=torch.uint8, device=device)
         self.bias = torch.zeros(self._i_bias.numel(), dtype=torch.float32, device=device)
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self.bwd = None
         self._i_bwd = None
-        if "bwd" in maps and bf16:
+        if "bwd" in maps and self.bf16:
             self._i_bwd = maps["bwd"].to(device)
-            self.bwd = (torch.zeros(self._i_bwd.numel() * 2, dtype=torch.uint8, device=device),
+            self.bwd = (torch.zeros(self.terms * self._i_bwd.numel() * 2, dtype=torch.uint8, device=device),
                         maps["bwd_table"].contiguous())
         self.version = None
 
     @staticmethod
-    def from_decoder(decoder: Decoder, device, bf16: bool = True) -> "TcWeights":
-        tw = TcWeights(decoder.kind, decoder.channels, device, bf16)
+    def from_decoder(decoder: Decoder, device, bf16: bool = True, mode: str | None = None) -> "TcWeights":
+        tw = TcWeights(decoder.kind, decoder.channels, device, bf16, mode)
         tw.refresh(pack_plain(decoder).to(device))
         return tw
+
+    def _fill(self, blob: torch.Tensor, values: torch.Tensor) -> None:
+        if self.terms == 1:
+            blob.view(self.dtype).copy_(values)
+            return
+        n = values.numel()
+        for i, t in enumerate(split_terms(values, self.terms)):
+            blob.view(torch.bfloat16)[i * n:(i + 1) * n].copy_(t)
 
     def refresh(self, params: torch.Tensor) -> None:
         """Rebuilds the images from the packed plain parameters (device ops only)."""
         p = params.detach().reshape(-1)
         ext = torch.cat([p.new_zeros(1), p])
-        self.blob.view(self.dtype).copy_(ext[self._i_fwd])
+        self._fill(self.blob, ext[self._i_fwd])
         self.bias.copy_(ext[self._i_bias])
         if self.bwd is not None:
-            self.bwd[0].view(self.dtype).copy_(ext[self._i_bwd])
+            self._fill(self.bwd[0], ext[self._i_bwd])
 
     def save_buffer(self, kind: int, channels: int, n_seg: int, device) -> torch.Tensor | None:
         """Buffer for the forward's layer inputs, read back by the tensor-core
         backward (None when this decoder / form has no tensor-core backward)."""
         if self.bwd is None:
             return None
-        n = int(N.lib().dv_decode_tc_save_bytes(kind, channels, n_seg))
+        fn = "dv_decode_tc_split_save_bytes" if self.terms > 1 else "dv_decode_tc_save_bytes"
+        n = int(getattr(N.lib(), fn)(kind, channels, n_seg))
         return torch.empty(max(n, 16), dtype=torch.uint8, device=device)
 
     def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st, saved=None, out4=None) -> bool:
-        """Tensor-core backward (DIVeR32, BF16); False when this decoder / form
-        has none (the caller then runs the FP32 CUDA backward).  With `saved`
-        (the forward's save buffer) and its `out4` the forward is read back
-        instead of recomputed."""
-        if self.bwd is None:
+        """Tensor-core backward (DIVeR32, BF16 / split BF16); False when this
+        decoder / form has none (the caller then runs the FP32 CUDA backward).
+        With `saved` (the forward's save buffer) and its `out4` the forward is
+        read back instead of recomputed; the split form requires it."""
+        if self.bwd is None or (self.terms > 1 and saved is None):
             return False
         nx, ny, nz, c = _grid(voxels)
         wb, tb = self.bwd
+        if self.terms > 1:
+            _timed("dv_decode_bwd_tc_split", kind, c, N.ptr(wb), wb.numel() // self.terms, tb.data_ptr(),
+                   tb.shape[0], nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr,
+                   N.ptr(pe_feat), N.ptr(d4), N.ptr(saved), saved.numel(), N.ptr(out4), N.ptr(gv), N.ptr(gp),
+                   N.ptr(self.err), st)
+            return True
         _timed("dv_decode_bwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), N.ptr(wb), wb.numel(), tb.data_ptr(), tb.shape[0],
                N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_feat),
@@ -126,6 +166,12 @@ class TcWeights:
 
     def decode(self, kind, channels, voxels, seg, pe_out, out4, st, voxels16=None, save=None):
         nx, ny, nz, c = _grid(voxels)
+        if self.terms > 1:
+            _timed("dv_decode_fwd_tc_split", kind, c, N.ptr(self.blob), self.term_bytes, N.ptr(self.bias),
+                   self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), nx, ny, nz,
+                   N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_out), N.ptr(out4),
+                   N.ptr(save), 0 if save is None else save.numel(), N.ptr(self.err), st)
+            return
         _timed("dv_decode_fwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), self.table.shape[0], N.ptr(voxels), N.ptr(voxels16),
                nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr, N.ptr(pe_out), N.ptr(out4),
@@ -253,15 +299,18 @@ class DIVeRField(torch.nn.Module):
         self.refresh_always = False
 
     def tc_weights(self, form: str) -> TcWeights | None:
-        """Tensor-core weights for form 'bf16' / 'fp16' (None for 'fp32'),
-        refreshed on the device whenever the decoder parameters changed (or on
-        every call while `refresh_always` is set, as inside a captured graph,
-        so that each replay packs the parameters of that moment)."""
+        """Tensor-core weights for form 'bf16' / 'fp16' / 'bf16s' (None for
+        'fp32'), refreshed on the device whenever the decoder parameters
+        changed (or on every call while `refresh_always` is set, as inside a
+        captured graph, so that each replay packs the parameters of that
+        moment)."""
+        if form not in FORMS:
+            raise ValueError(f"unknown decoder form {form!r} (one of {FORMS})")
         if form == "fp32":
             return None
         tw = self._tc.get(form)
         if tw is None:
-            tw = self._tc[form] = TcWeights(self.kind, self.voxels.shape[-1], self.voxels.device, form == "bf16")
+            tw = self._tc[form] = TcWeights(self.kind, self.voxels.shape[-1], self.voxels.device, mode=form)
         if self.refresh_always or tw.version != self.params._version:
             tw.refresh(self.params)
             tw.version = self.params._version
@@ -291,8 +340,9 @@ class DIVeRField(torch.nn.Module):
 
     def grid16(self, form: str) -> torch.Tensor | None:
         """BF16/FP16 copy of the feature grid for tensor-core rendering (made
-        once per grid version; None for the FP32 form)."""
-        if form == "fp32":
+        once per grid version; None for the FP32 and split forms, which read
+        the FP32 grid)."""
+        if form in ("fp32", "bf16s"):
             return None
         key = ("grid16", form, self.voxels._version)
         if getattr(self, "_g16key", None) != key:
@@ -332,8 +382,9 @@ class DIVeRField(torch.nn.Module):
     def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None,
                 grad_voxels=None):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
-        form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder).  Without
-        autograd the tensor-core forms read a 16-bit copy of the grid.
+        form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder; without
+        autograd they read a 16-bit copy of the grid) or 'bf16s' (tensor-core
+        decoder with split BF16 operands: FP32-grade, the accurate training form).
         capacity: fixed segment buffers, no host synchronisation (see segments).
         grad_voxels: see render_segments."""
         os, ds = os.contiguous(), ds.contiguous()

@@ -304,6 +304,30 @@ DV_API int dv_wait_selftest(int limit, int* status, void* stream);
 DV_API long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg);
 
 /*
+ * Split-operand form of dv_decode_fwd_tc (no counterpart in the reference,
+ * whose decoder runs FP32 torch GEMMs): FP32-grade products on BF16 tensor
+ * cores.  Every FP32 operand (the integrated features, each layer's
+ * activations, the weights) is carried as three BF16 terms, each rounding what
+ * the previous ones left, and each layer sums the six products whose term
+ * indices add up to at most 2 in FP32 accumulators (about 2^-24 relative per
+ * product).  wblob holds three terms of the images of dv_decode_fwd_tc, one
+ * after the other, wbytes apart (wbytes = one term's bytes); `layers`, bias and
+ * the rest as dv_decode_fwd_tc; the corner rows come from the FP32 grid.  save
+ * (optional, >= dv_decode_tc_split_save_bytes): receives every layer input as
+ * two BF16 terms for dv_decode_bwd_tc_split.
+ */
+DV_API int dv_decode_fwd_tc_split(int kind, int channels, const void* wblob, int wbytes,
+                                  const float* bias, int nbias, const int* layers, int n_layers,
+                                  const float* voxels, int nvx, int nvy, int nvz, const float* seg,
+                                  const int* seg_ray, long long n_seg, const int64_t* n_seg_dev,
+                                  const float* pe_out, float* out4, void* save,
+                                  long long save_capacity, int* err, void* stream);
+
+/* Bytes of the `save` buffer of dv_decode_fwd_tc_split for n_seg segments:
+ * per tile of 128 segments, every layer input tile as two BF16 terms. */
+DV_API long long dv_decode_tc_split_save_bytes(int kind, int channels, long long n_seg);
+
+/*
  * Allocation-free form of dv_exclusive_scan (no counterpart in the reference,
  * which allocates all its buffers with torch).  For callers that cannot
  * allocate device memory themselves — an embedding host whose allocator owns
@@ -339,6 +363,25 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
                             const float* pe_out, const float* d4, const void* saved,
                             long long saved_bytes, const float* out4, float* grad_voxels,
                             float* grad_params, int* err, void* stream);
+
+/*
+ * Split-operand form of dv_decode_bwd_tc (DIVeR32, 32 channels; no
+ * counterpart in the reference): FP32-grade gradients on BF16 tensor cores.
+ * Deltas propagate through three BF16 terms of each transposed weight image
+ * (wb: three terms of dv_decode_bwd_tc's images, wb_term_bytes apart;
+ * b_layers: HOST rows of (byte offset inside a term, K, N)) with six products
+ * per layer; weight gradients accumulate in FP32 from two-term deltas and
+ * activations (three products).  saved: the record dv_decode_fwd_tc_split
+ * wrote for the same segments and weights (saved_bytes >=
+ * dv_decode_tc_split_save_bytes), out4 its output; the forward is read back,
+ * never recomputed.  Adds into grad_voxels and grad_params like dv_decode_bwd.
+ */
+DV_API int dv_decode_bwd_tc_split(int kind, int channels, const void* wb, int wb_term_bytes,
+                                  const int* b_layers, int n_layers, int nvx, int nvy, int nvz,
+                                  const float* seg, const int* seg_ray, long long n_seg,
+                                  const int64_t* n_seg_dev, const float* pe_feat, const float* d4,
+                                  const void* saved, long long saved_bytes, const float* out4,
+                                  float* grad_voxels, float* grad_params, int* err, void* stream);
 
 /* Clearing a grid gradient where a step wrote it (no counterpart in the
  * reference, whose optimizer zeroes the whole dense gradient every step).

@@ -63,34 +63,44 @@ def test_integrate_backward_matches_autograd(g):
     assert np.abs(vox.grad.cpu().numpy() - ref).max() < 1e-5 * max(1.0, np.abs(ref).max())
 
 
-def run_field(g, kind):
+def run_field(g, kind, form="fp32"):
+    """Forward + backward of the golden case through render_segments with the
+    given decoder form ('fp32' plain kernels, or a tensor-core form)."""
     from diver_gb300 import masked_segments
     from diver_gb300.decoder import pack_plain
-    from diver_gb300.renderer import render_segments
+    from diver_gb300.renderer import TcWeights, render_segments
 
+    dec = decoder_from_golden(g, kind)
     vox = torch.from_numpy(g["voxels"]).cuda().requires_grad_(True)
-    params = pack_plain(decoder_from_golden(g, kind)).cuda().requires_grad_(True)
+    params = pack_plain(dec).cuda().requires_grad_(True)
+    tc = None if form == "fp32" else TcWeights.from_decoder(dec, "cuda", mode=form)
     o = torch.from_numpy(g["o_hit"]).cuda()
     d = torch.from_numpy(g["d_hit"]).cuda()
     seg = masked_segments(o, d, -1.5, 12, 0.25, torch.from_numpy(g["mask"]).cuda(), 1.0)
-    rgb, reg = render_segments(vox, params, seg, d, kind)
+    rgb, reg = render_segments(vox, params, seg, d, kind, True, tc)
     loss = torch.nn.functional.mse_loss(rgb, torch.from_numpy(g["target"]).cuda()) + 1e-5 * reg
     loss.backward()
+    torch.cuda.synchronize()
+    if tc is not None:
+        assert int(tc.err.item()) == 0
     return rgb, reg, loss, vox, params, seg
 
 
-@pytest.mark.parametrize("kind", ["diver32", "diver64"])
-def test_forward_and_loss_match_reference(g, kind):
-    rgb, reg, loss, *_ = run_field(g, kind)
+def check_forward_and_loss(g, kind, form="fp32"):
+    rgb, reg, loss, *_ = run_field(g, kind, form)
     assert np.abs(rgb.detach().cpu().numpy() - g[f"{kind}/rgb"]).max() < 1e-5
     assert abs(loss.item() - float(g[f"{kind}/loss"])) < 1e-6
 
 
 @pytest.mark.parametrize("kind", ["diver32", "diver64"])
-def test_gradients_match_reference_autograd(g, kind):
+def test_forward_and_loss_match_reference(g, kind):
+    check_forward_and_loss(g, kind)
+
+
+def check_gradients_vs_reference_autograd(g, kind, form="fp32"):
     from diver_gb300.decoder import unpack_plain_grad
 
-    _, _, _, vox, params, _ = run_field(g, kind)
+    _, _, _, vox, params, _ = run_field(g, kind, form)
     gv = vox.grad.reshape(-1, vox.shape[-1]).cpu().numpy()
     rows = g[f"{kind}/grad_voxels_rows"]
     ref = g[f"{kind}/grad_voxels"]
@@ -108,12 +118,16 @@ def test_gradients_match_reference_autograd(g, kind):
 
 
 @pytest.mark.parametrize("kind", ["diver32", "diver64"])
-def test_gradients_match_fp64_central_differences(g, kind):
+def test_gradients_match_reference_autograd(g, kind):
+    check_gradients_vs_reference_autograd(g, kind)
+
+
+def check_gradients_vs_central_differences(g, kind, form="fp32"):
     """Central differences of the FP64 oracle loss (same segments) for sampled
     feature entries and decoder weights: relative error <= 1e-4."""
     from diver_gb300.decoder import unpack_plain_grad
 
-    _, _, _, vox, params, seg = run_field(g, kind)
+    _, _, _, vox, params, seg = run_field(g, kind, form)
     gv = vox.grad.cpu().double()
     gp = unpack_plain_grad(kind, 32, params.grad.cpu())
     dec = decoder_from_golden(g, kind)
@@ -165,6 +179,12 @@ def test_gradients_match_fp64_central_differences(g, kind):
     assert rel < 1e-4, rel
     big = np.abs(fd) > 1e-2 * np.abs(fd).max()
     assert (np.abs(got - fd)[big] <= 1e-4 * np.abs(fd)[big] + 1e-9).all()
+    return rel
+
+
+@pytest.mark.parametrize("kind", ["diver32", "diver64"])
+def test_gradients_match_fp64_central_differences(g, kind):
+    check_gradients_vs_central_differences(g, kind)
 
 
 def test_render_small_scene_matches_fp64_oracle():
