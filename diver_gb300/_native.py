@@ -37,6 +37,7 @@ SIGNATURES = {
     "dv_dense_pair_counts": (I32, [I32, P, P, P]),
     "dv_camera_rays": (I32, [I32, I32, F32, P, I64, I64, P, P, P]),
     "dv_scan_scratch_bytes": (I64, [I64]),
+    "dv_walk_cap_hits": (I64, [I32]),
     "dv_exclusive_scan": (I32, [P, I64, P, P, P]),
     "dv_exclusive_scan_static_max": (I64, []),
     "dv_exclusive_scan_static": (I32, [P, I64, P, P]),

@@ -19,6 +19,28 @@
 
 namespace dv {
 
+// A direction with a non-finite component, or a zero direction, does not
+// advance one grid plane per step (its steps are NaN or -inf, and NaN points
+// never test as outside the grid): the walks treat such a ray as a miss.  The
+// reference kernels have no such check and never leave their loop on it.
+__device__ __forceinline__ bool dir_ok(const float3 d) {
+  return isfinite(d.x) && isfinite(d.y) && isfinite(d.z) && (d.x != 0.f || d.y != 0.f || d.z != 0.f);
+}
+
+// Step bound of a walk through a box of nx x ny x nz cells.  Every step snaps
+// one axis onto its next grid plane (the plane along the direction's sign,
+// strictly ahead of the point) and every coordinate moves monotonically, so a
+// ray crosses at most n + 1 planes per axis before it leaves: no walk of a ray
+// that passes dir_ok takes more steps.  The walks stop there all the same and
+// count the stop (note_cap_hit), so that no arithmetic case can keep a thread
+// walking.
+__host__ __device__ __forceinline__ int walk_cap(float nx, float ny, float nz) { return (int)(nx + ny + nz) + 3; }
+
+// Walks (of this translation unit) that stopped at walk_cap; read by
+// dv_walk_cap_hits.
+static __device__ unsigned long long g_walk_cap_hits;
+__device__ __forceinline__ void note_cap_hit() { atomicAdd(&g_walk_cap_hits, 1ull); }
+
 // Sign of x as -1, 0 or +1 (reference ray_voxel_intersect.cu:9-13).
 __device__ __forceinline__ float step_sign(float x) {
   return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);

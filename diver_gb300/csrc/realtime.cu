@@ -238,7 +238,13 @@ __device__ __forceinline__ void rt_frame_ray(const RtFrameArgs& a, const float* 
   int m = a.N / 64;
   long long off = 0;
   float3 last = p;
+  const int ocap = walk_cap((float)a.N, 0.f, 0.f) + 6;  // all octree levels (see octree_descend)
+  int steps = 0;
   while (m < a.N) {
+    if (steps++ == ocap) {
+      note_cap_hit();
+      return;
+    }
     last = p;
     float3 q;
     float dt;
@@ -263,10 +269,17 @@ __device__ __forceinline__ void rt_frame_ray(const RtFrameArgs& a, const float* 
   // decoding each hit as it is found would make every DDA step wait for the
   // lanes that decode.
   float* hits = hit_slots;  // [8][6] per thread
+  const int cap = walk_cap(n, n, n);  // the fine walk over all rounds
+  steps = 0;
   while (true) {
     int nh = 0;
     bool out = false;
     while (nh < 8) {
+      if (steps++ == cap) {
+        note_cap_hit();
+        out = true;
+        break;
+      }
       float3 q;
       float dt;
       grid_step<FAST>(last, d, r, s, q, dt);
@@ -311,7 +324,7 @@ __global__ void __launch_bounds__(128) rt_frame_kernel(const RtFrameArgs a) {
   const float3 d = make_float3(__ldg(a.v + 3 * b), __ldg(a.v + 3 * b + 1), __ldg(a.v + 3 * b + 2));
   float3 p = make_float3(__ldg(a.center), __ldg(a.center + 1), __ldg(a.center + 2));
   float t;
-  if (box_entry(p, d, (float)a.N, t)) {
+  if (dir_ok(d) && box_entry(p, d, (float)a.N, t)) {
     p = make_float3(__fmul_rn(p.x, 0.015625f), __fmul_rn(p.y, 0.015625f), __fmul_rn(p.z, 0.015625f));
     if (a.N < (1 << 22) && recip_ok(d))
       rt_frame_ray<W, FIRST, true>(a, sw, X, H, hit_slots, b, p, d, acc);
@@ -346,6 +359,15 @@ int launch_rt_frame(const RtFrameArgs& a, cudaStream_t st) {
 }  // namespace dv
 
 using namespace dv;
+
+// Walks of this file's kernels that stopped at their step bound (summed by
+// dv_walk_cap_hits in traverse.cu).
+long long realtime_walk_cap_hits(int reset) {
+  unsigned long long v = 0, w = 0;
+  if (cudaMemcpyFromSymbol(&v, g_walk_cap_hits, sizeof(v)) != cudaSuccess) return -1;
+  if (reset && cudaMemcpyToSymbol(g_walk_cap_hits, &w, sizeof(w)) != cudaSuccess) return -1;
+  return (long long)v;
+}
 
 extern "C" {
 

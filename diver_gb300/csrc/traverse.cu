@@ -83,7 +83,9 @@ __device__ __forceinline__ int dense_walk(const WalkArgs& a, int b, float3 p, co
   int count = 1;
   float3 q;
   float dt;
-  while (true) {
+  const int step_cap = walk_cap(a.n, a.n, a.n);
+  int k = 0;
+  for (; k < step_cap; ++k) {
     grid_step<FAST>(p, d, r, s, q, dt);
     const float tq = __fadd_rn(t, dt);
     if (outside_closed(q, a.n)) break;
@@ -105,6 +107,7 @@ __device__ __forceinline__ int dense_walk(const WalkArgs& a, int b, float3 p, co
     p = q;
     t = tq;
   }
+  if (k == step_cap) note_cap_hit();
   return count;
 }
 
@@ -117,7 +120,7 @@ __global__ void __launch_bounds__(256) dense_walk_kernel(const WalkArgs a) {
     const float3 d = load3(a.v, b);
     float3 p = ray_origin_voxel(a.o, b, a.xyzmin, a.voxel_size);
     float t;
-    const bool hit = box_entry(p, d, a.n, t);
+    const bool hit = dir_ok(d) && box_entry(p, d, a.n, t);
     float* row = nullptr;
     float* trow = nullptr;
     int64_t base = 0, cap = 0;
@@ -230,7 +233,9 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
   // steps taken so far, the step of the last occupied voxel (counting), and
   // where the walk may stop (emitting: nothing occupied lies beyond it)
   int steps = 0, last = 0;
-  const int limit = (MODE == WALK_SEGMENTS && a.stop_step) ? a.stop_step[b] : 0x7fffffff;
+  const int step_cap = walk_cap(a.n3.x, a.n3.y, a.n3.z);
+  const int limit = min((MODE == WALK_SEGMENTS && a.stop_step) ? a.stop_step[b] : 0x7fffffff, step_cap);
+  bool left = false;  // the walk left the grid
   while (!done) {
     float3 P[LOOKAHEAD + 1];
     float T[LOOKAHEAD];
@@ -249,6 +254,7 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
         t = __fadd_rn(t, dt);
         if (outside_closed3(q, a.n3)) {
           done = true;
+          left = true;
         } else {
           P[k + 1] = q;
           T[k] = t;
@@ -282,6 +288,7 @@ __device__ __forceinline__ int masked_walk(const WalkArgs& a, int b, float3 p, c
     }
     p = P[LOOKAHEAD];  // only read again when all LOOKAHEAD steps stayed inside
   }
+  if (!left && steps >= step_cap) note_cap_hit();
   if (MODE == WALK_SEGMENTS || MODE == WALK_SLOTS) w.flush(a, b);
   if (MODE == WALK_COUNT && a.last_step) a.last_step[b] = last;
   return count;
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(256) masked_walk_kernel(const WalkArgs a) {
     const float3 d = load3(a.v, b);
     float3 p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
     float t;
-    if (box_entry3(p, d, a.n3, t))
+    if (dir_ok(d) && box_entry3(p, d, a.n3, t))
       count = (a.fast && recip_ok(d)) ? masked_walk<MODE, true, K>(a, b, p, d, t)
                                       : masked_walk<MODE, false, K>(a, b, p, d, t);
     else if (MODE == WALK_COUNT && a.last_step)
@@ -346,7 +353,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
   if (b < a.batch) {
     d = load3(a.v, b);
     p = ray_origin_voxel3(a.o, b, a.o3, a.voxel_size);
-    if (box_entry3(p, d, a.n3, t)) {
+    if (dir_ok(d) && box_entry3(p, d, a.n3, t)) {
       done = false;
       fast = a.fast && recip_ok(d);
       r = fast ? recip3(d) : d;
@@ -358,7 +365,9 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
   int nb = 0;         // staged segments of this lane
   int64_t g = base;   // global index of the first staged one
   int steps = 0;      // walk steps taken; nothing occupied lies beyond `limit`
-  const int limit = (!done && a.stop_step) ? a.stop_step[b] : 0x7fffffff;
+  const int step_cap = walk_cap(a.n3.x, a.n3.y, a.n3.z);
+  const int limit = min((!done && a.stop_step) ? a.stop_step[b] : 0x7fffffff, step_cap);
+  bool left = false;  // the walk left the grid
   while (__any_sync(0xffffffffu, !done) || __any_sync(0xffffffffu, nb > 0)) {
     if (!done) {
       float3 P[K + 1];
@@ -377,6 +386,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
           t = __fadd_rn(t, dt);
           if (outside_closed3(q, a.n3)) {
             done = true;
+            left = true;
           } else {
             P[k + 1] = q;
             T[k] = t;
@@ -425,6 +435,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) masked_emit_staged_kernel(const
     nb = 0;
     __syncwarp();
   }
+  if (b < a.batch && steps > 0 && !left && steps >= step_cap) note_cap_hit();
 }
 
 // Slots -> CSR: row k of ray b moves from b * slot + k to offsets[b] + k.
@@ -457,7 +468,16 @@ __device__ __forceinline__ void octree_descend(float* slot, uint8_t* finish, int
   int m = N / 64;
   long long off = 0;
   float3 last = p;
+  // the levels walk fewer than 3 (N/64 + N/16 + N/4) + 9 <= N + 9 steps in all
+  const int cap = walk_cap((float)N, 0.f, 0.f) + 6;
+  int steps = 0;
   while (m < N) {
+    if (steps++ == cap) {
+      note_cap_hit();
+      slot[0] = -1.f;
+      finish[b] = 1;
+      return;
+    }
     last = p;
     float3 q;
     float dt;
@@ -497,7 +517,7 @@ __global__ void __launch_bounds__(256) aabb_kernel(int batch, float* __restrict_
   const float3 d = load3(v, b);
   float3 p = make_float3(__ldg(center + 0), __ldg(center + 1), __ldg(center + 2));
   float t;
-  if (!box_entry(p, d, (float)N, t)) {
+  if (!dir_ok(d) || !box_entry(p, d, (float)N, t)) {
     slot[0] = -1.f;
     finish[b] = 1;
     return;
@@ -520,8 +540,14 @@ __device__ __forceinline__ void march8(float* __restrict__ coords, long long str
   const float3 r = FAST ? recip3(d) : d;
   const float n = (float)N;
   const long long cells = (long long)N * N * N;
-  int hits = 0;
+  const int cap = walk_cap(n, n, n);
+  int hits = 0, steps = 0;
   while (hits < 8) {
+    if (steps++ == cap) {
+      note_cap_hit();
+      coords[hits * stride + (long long)b * 6] = -1.f;
+      break;
+    }
     float3 q;
     float dt;
     grid_step<FAST>(last, d, r, s, q, dt);
@@ -552,6 +578,7 @@ __global__ void __launch_bounds__(256) march_kernel(int batch, float* __restrict
   coords[(long long)b * 6] = -1.f;
   if (last.x < 0.f) return;
   const float3 d = load3(v, b);
+  if (!dir_ok(d)) return;  // a miss (aabb_intersect finished such a ray already)
   const float lim = (float)N;  // a resume point from outside the grid takes the __fdiv_rn form
   if (N < (1 << 22) && recip_ok(d) && fabsf(last.x) <= lim && fabsf(last.y) <= lim && fabsf(last.z) <= lim)
     march8<true>(coords, stride, b, last, d, mask, N);
@@ -674,6 +701,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_tiles(const int* __restrict
 }  // namespace dv
 
 using namespace dv;
+
+long long realtime_walk_cap_hits(int reset);  // realtime.cu
 
 // int(voxel_num * mask_scale) with the product rounded to float first, as the
 // reference computes it on the device (ray_voxel_intersect.cu:268).
@@ -962,6 +991,15 @@ int dv_masked_segments_grid(int batch_size, const float* xyzmin, const int* dims
     DV_WALK_LAUNCH(masked_walk_kernel<WALK_SEGMENTS>, batch_size, stream, a);
   DV_TRY_LAUNCH();
   return DV_OK;
+}
+
+long long dv_walk_cap_hits(int reset) {
+  unsigned long long v = 0, w = 0;
+  if (cudaMemcpyFromSymbol(&v, g_walk_cap_hits, sizeof(v)) != cudaSuccess) return -1;
+  const long long rt = realtime_walk_cap_hits(reset);
+  if (rt < 0) return -1;
+  if (reset && cudaMemcpyToSymbol(g_walk_cap_hits, &w, sizeof(w)) != cudaSuccess) return -1;
+  return (long long)v + rt;
 }
 
 long long dv_scan_scratch_bytes(long long n) {

@@ -157,6 +157,16 @@ DV_API int dv_dense_pair_counts(int batch_size, const int* intersect_num, int* s
  * Exclusive prefix sum of n int32 counts into n+1 int64 offsets
  * (offsets[n] = total).  scratch must hold dv_scan_scratch_bytes(n) bytes.
  */
+/* Walks that stopped at their step bound since the last reset (no
+ * counterpart in the reference, whose walks have no bound).  Every walk
+ * (dense, masked, octree first hit, 8-hit march, the real-time frame) stops
+ * after nx + ny + nz + 3 grid-plane steps, which no ray with a finite, nonzero
+ * direction reaches (each step crosses one plane); rays with a non-finite or
+ * zero direction are misses.  A nonzero count means some arithmetic case
+ * broke that bound and its walk was cut short.  Synchronous (reads device
+ * counters of the current device); reset = 1 zeroes them; -1 on a CUDA error. */
+DV_API long long dv_walk_cap_hits(int reset);
+
 DV_API long long dv_scan_scratch_bytes(long long n);
 DV_API int dv_exclusive_scan(const int* counts, long long n, int64_t* offsets, void* scratch,
                       void* stream);

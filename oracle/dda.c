@@ -19,6 +19,28 @@
 
 typedef struct { float x, y, z; } v3;
 
+/* Walks that stopped at their step bound (see walk_cap). */
+static long long cap_hits = 0;
+
+/* A direction with a non-finite component, or a zero direction, does not
+ * advance one grid plane per step (its steps are NaN or -inf and the walk
+ * would never leave the grid): such a ray is a miss.  The reference kernels
+ * have no such check and loop forever on it. */
+static int dir_ok(v3 d) {
+  return isfinite(d.x) && isfinite(d.y) && isfinite(d.z) && (d.x != 0.f || d.y != 0.f || d.z != 0.f);
+}
+
+/* Step bound of a walk through a box of nx x ny x nz cells: every step snaps
+ * one axis onto its next grid plane and the coordinates move monotonically,
+ * so a ray crosses at most n + 1 planes per axis before it leaves. */
+static int walk_cap(float nx, float ny, float nz) { return (int)(nx + ny + nz) + 3; }
+
+long long oracle_walk_cap_hits(int reset) {
+  long long v = cap_hits;
+  if (reset) cap_hits = 0;
+  return v;
+}
+
 static float sgnf(float x) { return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f); }
 static float clampf(float v, float lo, float hi) { return fmaxf(lo, fminf(v, hi)); }
 static float madd(float a, float b, float c, int fused) {
@@ -98,7 +120,7 @@ void oracle_dense_walk(int batch, int max_n, float xyzmin, float n, float vs, co
     v3 d = {v[3 * b], v[3 * b + 1], v[3 * b + 2]};
     v3 p = {(o[3 * b] - xyzmin) / vs, (o[3 * b + 1] - xyzmin) / vs, (o[3 * b + 2] - xyzmin) / vs};
     float t;
-    int hit = box_entry(&p, d, n, &t, fused);
+    int hit = dir_ok(d) && box_entry(&p, d, n, &t, fused);
     float* row = inter + (long long)b * max_n * 3;
     float* trow = tns + (long long)b * max_n;
     int count = 0;
@@ -111,7 +133,9 @@ void oracle_dense_walk(int batch, int max_n, float xyzmin, float n, float vs, co
       if (max_n > 0) trow[0] = t * vs;
       count = 1;
       v3 s = {sgnf(d.x), sgnf(d.y), sgnf(d.z)};
-      for (;;) {
+      const int cap = walk_cap(n, n, n);
+      int k = 0;
+      for (; k < cap; ++k) {
         float dt;
         v3 q = grid_step(p, d, s, &dt, fused);
         t = t + dt;
@@ -125,6 +149,7 @@ void oracle_dense_walk(int batch, int max_n, float xyzmin, float n, float vs, co
         ++count;
         p = q;
       }
+      if (k == cap) ++cap_hits;
     }
     num[b] = count;
   }
@@ -142,11 +167,13 @@ void oracle_masked_walk(int batch, int max_n, float xyzmin, float n, float vs, f
     v3 p = {(o[3 * b] - xyzmin) / vs, (o[3 * b + 1] - xyzmin) / vs, (o[3 * b + 2] - xyzmin) / vs};
     float t;
     int count = 0;
-    if (box_entry(&p, d, n, &t, fused)) {
+    if (dir_ok(d) && box_entry(&p, d, n, &t, fused)) {
       v3 s = {sgnf(d.x), sgnf(d.y), sgnf(d.z)};
       float* row = inter + (long long)b * max_n * 6;
       float* trow = tns + (long long)b * max_n;
-      for (;;) {
+      const int cap = walk_cap(n, n, n);
+      int k = 0;
+      for (; k < cap; ++k) {
         float dt;
         v3 q = grid_step(p, d, s, &dt, fused);
         t = t + dt;
@@ -162,6 +189,7 @@ void oracle_masked_walk(int batch, int max_n, float xyzmin, float n, float vs, f
         }
         p = q;
       }
+      if (k == cap) ++cap_hits;
     }
     num[b] = count;
   }
@@ -180,7 +208,7 @@ void oracle_aabb(int batch, float* coords, const float* v, const float* center, 
     v3 d = {v[3 * b], v[3 * b + 1], v[3 * b + 2]};
     v3 p = {center[0], center[1], center[2]};
     float t;
-    if (!box_entry(&p, d, (float)N, &t, fused)) {
+    if (!dir_ok(d) || !box_entry(&p, d, (float)N, &t, fused)) {
       slot[0] = -1.f;
       finish[b] = 1;
       continue;
@@ -191,7 +219,17 @@ void oracle_aabb(int batch, float* coords, const float* v, const float* center, 
     long long off = 0;
     v3 last = p;
     int missed = 0;
+    /* every level walks fewer than 3 (N / 4) + 3 steps */
+    const int cap = walk_cap((float)N, 0.f, 0.f) + 6;
+    int steps = 0;
     while (m < N) {
+      if (steps++ == cap) {
+        ++cap_hits;
+        slot[0] = -1.f;
+        finish[b] = 1;
+        missed = 1;
+        break;
+      }
       last = p;
       float dt;
       v3 q = grid_step(last, d, s, &dt, fused);
@@ -231,9 +269,17 @@ void oracle_ray_march(int batch, float* coords, const float* v, const uint8_t* m
     coords[(long long)b * 6] = -1.f;
     if (last.x < 0.f) continue;
     v3 d = {v[3 * b], v[3 * b + 1], v[3 * b + 2]};
+    if (!dir_ok(d)) continue;
     v3 s = {sgnf(d.x), sgnf(d.y), sgnf(d.z)};
     int hits = 0;
+    const int cap = walk_cap((float)N, (float)N, (float)N);
+    int steps = 0;
     while (hits < 8) {
+      if (steps++ == cap) {
+        ++cap_hits;
+        coords[hits * stride + (long long)b * 6] = -1.f;
+        break;
+      }
       float dt;
       v3 q = grid_step(last, d, s, &dt, fused);
       if (out_open(q, (float)N)) {
@@ -262,9 +308,9 @@ void oracle_masked_walk_grid(int batch, int max_n, const float* xyzmin, const in
     v3 d = {v[3 * b], v[3 * b + 1], v[3 * b + 2]};
     v3 p = {(o[3 * b] - xyzmin[0]) / vs, (o[3 * b + 1] - xyzmin[1]) / vs, (o[3 * b + 2] - xyzmin[2]) / vs};
     float t = 0.f;
-    int count = 0, hit = 1;
+    int count = 0, hit = dir_ok(d);
     int inside = (p.x >= 0.f) & (p.y >= 0.f) & (p.z >= 0.f) & (p.x <= nx) & (p.y <= ny) & (p.z <= nz);
-    if (!inside) {
+    if (hit && !inside) {
       float a = (-p.x) / d.x, c = (nx - p.x) / d.x;
       float lo = fminf(a, c), hi = fmaxf(a, c);
       a = (-p.y) / d.y; c = (ny - p.y) / d.y;
@@ -281,7 +327,9 @@ void oracle_masked_walk_grid(int batch, int max_n, const float* xyzmin, const in
       v3 s = {sgnf(d.x), sgnf(d.y), sgnf(d.z)};
       float* row = inter + (long long)b * max_n * 6;
       float* trow = tns + (long long)b * max_n;
-      for (;;) {
+      const int cap = walk_cap(nx, ny, nz);
+      int k = 0;
+      for (; k < cap; ++k) {
         float dt;
         v3 q = grid_step(p, d, s, &dt, 1);
         t = t + dt;
@@ -300,6 +348,7 @@ void oracle_masked_walk_grid(int batch, int max_n, const float* xyzmin, const in
         }
         p = q;
       }
+      if (k == cap) ++cap_hits;
     }
     num[b] = count;
   }

@@ -26,6 +26,8 @@ def lib():
         h.oracle_ray_march.argtypes = [I, P, P, P, P, I, I]
         for n in ("oracle_mlp_eval_f32", "oracle_mlp_eval_f64"):
             getattr(h, n).argtypes = [I, I, P, P, P, I, P, P, P, P]
+        h.oracle_walk_cap_hits.argtypes = [I]
+        h.oracle_walk_cap_hits.restype = C.c_longlong
         for n in ("oracle_dense_walk", "oracle_masked_walk", "oracle_aabb", "oracle_ray_march",
                   "oracle_mlp_eval_f32", "oracle_mlp_eval_f64"):
             getattr(h, n).restype = None
@@ -112,3 +114,8 @@ def mlp_eval(width, coords, feats, vmap, params, v, rgba, finish, double=False):
 def csr_from_padded(inter, num):
     """Rows [b, :num[b]] of a padded buffer, concatenated ray by ray (boolean-mask order)."""
     return np.concatenate([inter[b, :num[b]] for b in range(inter.shape[0])], 0) if inter.shape[0] else inter[:0, 0]
+
+
+def walk_cap_hits(reset: bool = True) -> int:
+    """Walks of the C restatement that stopped at their step bound since the last reset."""
+    return int(lib().oracle_walk_cap_hits(int(reset)))

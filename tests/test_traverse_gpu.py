@@ -175,6 +175,32 @@ def test_full_size_masked_is_occupancy_filter_of_dense():
     assert same_bits(inter.cpu().numpy(), oi) and same_bits(tns.cpu().numpy(), ot)
 
 
+def test_full_frame_walks_stay_within_their_step_bound():
+    """800x800 frames of the 256^3 scene through every walk (dense, masked
+    count + emission, captured slot walk, octree first hit + march rounds,
+    the one-launch real-time frame): no walk reaches its step bound."""
+    from diver_gb300 import _native as N
+    from diver_gb300 import dense_segments, masked_segments, scenes
+    from diver_gb300.realtime import RealtimeModel, convert
+    from diver_gb300.renderer import DIVeRField
+
+    N.lib().dv_walk_cap_hits(1)
+    sc = scenes.grid_scene(256, 32, device="cuda")
+    c2w = scenes.sphere_cameras(1, 4.0, 3)[0]
+    o, v = scenes.camera_rays(c2w, 800, 800, 960.0, "cuda")
+    dense_segments(o, v, sc.xyzmin, sc.voxel_num, sc.voxel_size)
+    masked_segments(o, v, sc.xyzmin, sc.voxel_num, sc.voxel_size, sc.mask, 1.0)
+    field = DIVeRField.from_scene(sc, "cuda")
+    field.segments(o[:4096].contiguous(), v[:4096].contiguous(), capacity=field.segment_capacity(4096))
+    sd = {"voxels": sc.features}
+    sd.update(sc.decoder.state_dict())
+    model = RealtimeModel.from_serialized(convert(sd, sc.mask.float()), 256, sc.xyzmin, sc.voxel_size, "cuda")
+    model.render_frame(c2w[:, 3].cuda(), v)
+    model.render_frame(c2w[:, 3].cuda(), v, fused=False)
+    torch.cuda.synchronize()
+    assert N.lib().dv_walk_cap_hits(1) == 0
+
+
 def test_empty_and_all_miss_batches():
     from diver_gb300 import masked_intersect, masked_segments, ray_voxel_intersect
 
