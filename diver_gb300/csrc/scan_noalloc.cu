@@ -16,9 +16,12 @@
 //     launch;
 //   - the array (32 KiB) exists on every device that loads the library and
 //     stays allocated until the process exits;
-//   - the first call on a device looks up the array's device address (a
-//     one-time set-up per device, made with that device current); make that
-//     first call before any stream capture;
+//   - the first call on a device with n > 0 looks up the array's device
+//     address (a one-time set-up per device, made with that device current);
+//     make that first call before any stream capture.  The address is cached
+//     for the process: after cudaDeviceReset (or any teardown of the device's
+//     primary context) the library must not be called on that device again;
+//   - n = 0 only writes offsets[0] = 0 and needs no set-up;
 //   - all calls share the one array: calls whose work overlaps on the GPU
 //     (different streams, or different host threads on the same device) race
 //     on it and must be serialised by the caller;
@@ -68,15 +71,15 @@ long long dv_exclusive_scan_static_max(void) { return DV_SCAN_STATIC_MAX_TILES *
 int dv_exclusive_scan_static(const int* counts, long long n, int64_t* offsets, void* stream) {
   DV_CHECK(n >= 0 && offsets, DV_ERR_ARG);
   if (n > DV_SCAN_STATIC_MAX_TILES * SCAN_TILE) return DV_ERR_OVERFLOW;
-  long long* tile_sum = nullptr;
-  const int st_setup = static_scratch(&tile_sum);
-  if (st_setup != DV_OK) return st_setup;
   cudaStream_t st = (cudaStream_t)stream;
   if (n == 0) {
     if (cudaMemsetAsync(offsets, 0, sizeof(int64_t), st) != cudaSuccess) return DV_ERR_CUDA;
     return DV_OK;
   }
   DV_CHECK(counts, DV_ERR_ARG);
+  long long* tile_sum = nullptr;
+  const int st_setup = static_scratch(&tile_sum);
+  if (st_setup != DV_OK) return st_setup;
   const long long tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
   scan_tile_sums<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(counts, n, tile_sum);
   scan_tile_prefix<<<1, SCAN_THREADS, 0, st>>>(tile_sum, tiles);

@@ -87,7 +87,12 @@ class TrainStepGraph:
         return loss.detach(), gv, gp
 
     def __call__(self, o: torch.Tensor, d: torch.Tensor, target: torch.Tensor):
-        """(loss, grad_voxels, grad_params) of this batch (graph buffers)."""
+        """(loss, grad_voxels, grad_params) of this batch: the graph's own
+        buffers, overwritten by the next replay.  With sparse clearing (the
+        default) only the grid-gradient rows a replay writes are zeroed before
+        the next one, so grad_voxels is read-only for the caller: clone it
+        before changing it (an optimizer or hook that adds into it in place
+        would carry its change into every later step)."""
         self.o.copy_(o, non_blocking=True)
         self.d.copy_(d, non_blocking=True)
         self.target.copy_(target, non_blocking=True)

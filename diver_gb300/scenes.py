@@ -243,28 +243,35 @@ def ellipse_cameras(count=150, a=3.0, b=2.0, z=0.8) -> list[torch.Tensor]:
 
 
 def training_batches(scene: Scene, count: int, batch: int, device, seed: int = 4, cameras: int = 100,
-                     size: int = 800, focal: float = 960.0):
+                     size: int = 800, focal: float = 960.0, count_fn=None):
     """`count` batches (o, d, target) of `batch` rays drawn from `cameras`
     sphere cameras (radius 4) at size x size pixels, kept only where the ray
     crosses at least one occupied voxel of the scene (cubic grids); targets
-    U[0, 1]."""
-    from . import _native as N
+    U[0, 1].  count_fn(o, d) -> per-ray counts of occupied segments (int
+    tensor on `device`); by default the CUDA masked walk (dv_masked_count)."""
+    if count_fn is None:
+        from . import _native as N
+
+        m8 = scene.mask.view(torch.uint8)
+
+        def count_fn(o, d):
+            num = torch.empty(d.shape[0], dtype=torch.int32, device=device)
+            N.call("dv_masked_count", d.shape[0], scene.xyzmin, float(scene.voxel_num), scene.voxel_size, 1.0,
+                   N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, None, N.stream(device))
+            return num
 
     cams = sphere_cameras(cameras, 4.0, 3)
     dirs_cam = pixel_directions(size, size, focal, device).reshape(-1, 3)
     g = torch.Generator(device=device).manual_seed(seed)
     gc = torch.Generator().manual_seed(seed)
     out = []
-    m8 = scene.mask.view(torch.uint8)
     while len(out) < count:
         c2w = cams[int(torch.randint(0, cameras, (1,), generator=gc))].to(device)
         pick = torch.randint(0, dirs_cam.shape[0], (3 * batch,), generator=g, device=device)
         d = dirs_cam[pick] @ c2w[:, :3].t()
         d = (d / d.norm(dim=-1, keepdim=True)).contiguous()
         o = c2w[:, 3].expand(d.shape).contiguous()
-        num = torch.empty(d.shape[0], dtype=torch.int32, device=device)
-        N.call("dv_masked_count", d.shape[0], scene.xyzmin, float(scene.voxel_num), scene.voxel_size, 1.0,
-               N.ptr(o), N.ptr(d), N.ptr(m8), N.ptr(num), None, None, N.stream(device))
+        num = count_fn(o, d)
         keep = torch.nonzero(num > 0)[:, 0]
         if keep.numel() < batch:
             continue

@@ -63,24 +63,35 @@ class SceneEntry:
 
 
 class Residency:
-    """HBM-budgeted scene residency with LRU eviction of idle scenes."""
+    """HBM-budgeted scene residency with LRU eviction of idle scenes.
+    `reserved_bytes` of the budget are set aside for the working memory of
+    the batches in flight (segment lists, decoder outputs); scenes are charged
+    the bytes given at registration (their grids, any 16-bit copy of the grid
+    the renderer makes, occupancy and weights) against the rest."""
 
-    def __init__(self, budget_bytes: int):
+    def __init__(self, budget_bytes: int, reserved_bytes: int = 0):
         self.budget = int(budget_bytes)
+        self.reserved = int(reserved_bytes)
+        if self.reserved >= self.budget:
+            raise ValueError("the reserved working memory leaves no HBM budget for scenes")
         self.scenes: dict[str, SceneEntry] = {}
         self.lru: OrderedDict[str, None] = OrderedDict()
         self.used = 0
 
+    @property
+    def scene_budget(self) -> int:
+        return self.budget - self.reserved
+
     def register(self, name: str, nbytes: int, loader) -> None:
-        if nbytes > self.budget:
-            raise ValueError(f"scene {name} ({nbytes} B) exceeds the HBM budget ({self.budget} B)")
+        if nbytes > self.scene_budget:
+            raise ValueError(f"scene {name} ({nbytes} B) exceeds the HBM budget for scenes ({self.scene_budget} B)")
         self.scenes[name] = SceneEntry(name, int(nbytes), loader)
 
     def acquire(self, name: str) -> bool:
         """Makes `name` resident (evicting idle scenes if needed); False if it cannot fit now."""
         e = self.scenes[name]
         if e.resident is None:
-            need = self.used + e.nbytes - self.budget
+            need = self.used + e.nbytes - self.scene_budget
             if need > 0:
                 victims = [n for n in self.lru if self.scenes[n].active == 0 and self.scenes[n].resident is not None]
                 freed = 0

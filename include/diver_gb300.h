@@ -346,10 +346,11 @@ DV_API long long dv_decode_tc_split_save_bytes(int kind, int channels, long long
  * library (present on every device that loads it, until the process exits).
  * n may be at most dv_exclusive_scan_static_max() (8,388,608 counts); larger
  * n returns DV_ERR_OVERFLOW without launching anything.  The first call on a
- * device looks up the array's address (once per device, with that device
- * current): make it before any stream capture.  Calls share the array, so
- * calls that overlap on the GPU race and must be serialised by the caller.
- * Calls no cudaMalloc/cudaFree.
+ * device with n > 0 looks up the array's address (once per device, with that
+ * device current): make it before any stream capture.  The address stays
+ * cached for the process, so the entry point must not be used on a device
+ * after cudaDeviceReset.  Calls share the array, so calls that overlap on the
+ * GPU race and must be serialised by the caller.  Calls no cudaMalloc/cudaFree.
  */
 DV_API long long dv_exclusive_scan_static_max(void);
 DV_API int dv_exclusive_scan_static(const int* counts, long long n, int64_t* offsets, void* stream);

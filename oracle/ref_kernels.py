@@ -2,7 +2,7 @@
 kernels, compiled from the reference sources in place and run through the
 CUDA driver API, to produce the traversal fixtures in tests/golden/.
 
-  build_cubins()  nvcc -cubin of utils/ray_voxel_intersection/src/
+  build_cubins(root)  nvcc -cubin of utils/ray_voxel_intersection/src/
                   ray_voxel_intersect.cu and utils/ray_march/src/ray_march.cu
                   with the reference's default nvcc flags (no fast math,
                   default -fmad=true) into oracle/_ref/*.cubin.  Needs the
@@ -21,7 +21,6 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("DIVER_REFERENCE", "/root/reference"))
 OUT = HERE / "_ref"
 UNITS = {
     "ray_voxel_intersect": "utils/ray_voxel_intersection/src/ray_voxel_intersect.cu",
@@ -29,11 +28,21 @@ UNITS = {
 }
 
 
-def build_cubins(force: bool = False) -> list[Path]:
-    """Compiles the reference kernels when the reference sources are present."""
+def reference_root(root: str | os.PathLike | None = None) -> Path | None:
+    """The reference source tree: `root`, else $DIVER_REFERENCE, else None."""
+    r = root if root is not None else os.environ.get("DIVER_REFERENCE")
+    return Path(r) if r else None
+
+
+def build_cubins(root: str | os.PathLike | None = None, force: bool = False) -> list[Path]:
+    """Compiles the reference kernels when the reference sources are present
+    (tree `root` or $DIVER_REFERENCE)."""
     out = []
+    ref = reference_root(root)
+    if ref is None:
+        return out
     for name, rel in UNITS.items():
-        src = REF_ROOT / rel
+        src = ref / rel
         dst = OUT / f"{name}.cubin"
         if not src.exists():
             continue

@@ -1,6 +1,8 @@
-"""ORACLE — test infrastructure only.  torch (CPU) restatement of the
-reference's training/offline decode path, used for reference gradients
-(autograd, float32 or float64) and as the timed CPU baseline:
+"""ORACLE — test infrastructure only.  torch restatement of the reference's
+training/offline decode path, used for reference gradients (autograd, float32
+or float64), as the timed CPU baseline, and (on CUDA tensors, fed by the
+reference's own traversal kernels) as the reference's GPU path in bench.py's
+reference arm:
 
   integrate     utils/integrator.py:62-112
   pos_enc       model/mlps.py:6-18 (L = 4 bands)
@@ -34,7 +36,7 @@ def integrate(voxels: torch.Tensor, coord_i: torch.Tensor, coord_o: torch.Tensor
     xmin, ymin, zmin = pmin.split(1, dim=-1)
     if per_axis:
         nz, ny, nx = voxels.shape[:3]
-        hi = torch.tensor([nx - 1, ny - 1, nz - 1])
+        hi = torch.tensor([nx - 1, ny - 1, nz - 1], device=coord_i.device)
         xmax, ymax, zmax = torch.minimum(pmin + 1, hi).split(1, dim=-1)
     else:
         xmax, ymax, zmax = (pmin + 1).clamp_max(n - 1).split(1, dim=-1)
@@ -87,8 +89,8 @@ def scatter_padded(values: torch.Tensor, counts: torch.Tensor, fill=0.0):
     """CSR values [S, ...] -> padded [B, M, ...] and mask [B, M] (ray-major order)."""
     B = counts.numel()
     M = int(counts.max().item()) if B else 0
-    mask = torch.arange(M)[None, :] < counts[:, None].long()
-    out = torch.full((B, M) + tuple(values.shape[1:]), fill, dtype=values.dtype)
+    mask = torch.arange(M, device=counts.device)[None, :] < counts[:, None].long()
+    out = torch.full((B, M) + tuple(values.shape[1:]), fill, dtype=values.dtype, device=values.device)
     out = out.clone()
     out[mask] = values
     return out, mask
@@ -109,6 +111,7 @@ def forward(voxels, layers, n_mlp1, seg, seg_ray, counts, dirs, white_back=True,
     """Full decode path over CSR segments: returns rgb [B,3], sigma [B,M], mask [B,M]."""
     feat = integrate(voxels, seg[:, :3], seg[:, 3:], per_axis, dtype)
     s, c = decode(layers, n_mlp1, feat, dirs[seg_ray.long()])
+    counts = counts.to(feat.device)
     sigma, mask = scatter_padded(s, counts)
     color, _ = scatter_padded(c, counts)
     rgb, _ = render(color, sigma, mask, white_back)

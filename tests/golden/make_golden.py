@@ -179,6 +179,8 @@ def make_convert(ref_root: Path, out: Path):
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path(os.environ.get("DIVER_REFERENCE", "/root/reference"))
+    if len(sys.argv) < 2 and not os.environ.get("DIVER_REFERENCE"):
+        sys.exit("usage: make_golden.py <reference tree> (or set DIVER_REFERENCE)")
+    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path(os.environ["DIVER_REFERENCE"])
     make_decode(ref, HERE / "decode_ref.npz")
     make_convert(ref, HERE / "convert_ref.npz")

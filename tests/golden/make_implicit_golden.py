@@ -13,6 +13,7 @@ to every MLP parameter.
 from __future__ import annotations
 
 import importlib.util
+import os
 import sys
 from pathlib import Path
 
@@ -65,4 +66,6 @@ def main(ref_root: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) < 2 and not os.environ.get("DIVER_REFERENCE"):
+        sys.exit("usage: make_implicit_golden.py <reference tree> (or set DIVER_REFERENCE)")
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path(os.environ["DIVER_REFERENCE"]))

@@ -137,3 +137,30 @@ def test_sparse_and_dense_clearing_steps_agree():
         # rows this batch does not write are exactly zero in both
         untouched = (gvd == 0).all(-1)
         assert int((gvs[untouched] != 0).sum().item()) == 0
+
+
+def test_caller_writes_to_the_returned_gradient_outside_the_written_rows_persist():
+    """The contract of the sparse-clearing captured step: its grid gradient
+    is the graph's own buffer and only the rows a replay writes are cleared
+    before the next one, so a caller that changes other rows of it (instead
+    of cloning first) sees the change in every later step."""
+    from diver_gb300 import scenes
+    from diver_gb300.graphs import TrainStepGraph
+    from diver_gb300.renderer import DIVeRField
+
+    sc = scenes.small_scene("cpu")
+    field = DIVeRField.from_scene(sc, "cuda")
+    o, d = scenes.small_view("cuda")
+    pick = torch.arange(0, o.shape[0], 37, device="cuda")[:1024]
+    tgt = torch.rand(pick.numel(), 3, generator=torch.Generator().manual_seed(2)).cuda()
+    step = TrainStepGraph(field, o[pick].contiguous(), d[pick].contiguous(), tgt, form="bf16s")
+    _, gv, _ = step(o[pick], d[pick], tgt)
+    torch.cuda.synchronize()
+    untouched = torch.nonzero((gv == 0).all(-1).reshape(-1))[:, 0]
+    assert untouched.numel() > 0
+    row = int(untouched[0])
+    gv.view(-1, gv.shape[-1])[row] = 1.0  # a caller write to a row the step does not write
+    _, gv2, _ = step(o[pick], d[pick], tgt)
+    torch.cuda.synchronize()
+    assert gv2.data_ptr() == gv.data_ptr()
+    assert bool((gv2.view(-1, gv2.shape[-1])[row] == 1.0).all())

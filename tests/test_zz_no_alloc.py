@@ -51,6 +51,24 @@ def test_static_scan_matches_allocating_scan_on_two_calls():
     assert torch.equal(b, allocating_scan(lib, second))
 
 
+def test_static_scan_at_its_limit_and_when_empty():
+    """n equal to the limit fills all 4096 tiles of the array; n = 0 writes
+    only offsets[0] = 0."""
+    from diver_gb300 import _native
+
+    lib = _native.lib()
+    limit = int(lib.dv_exclusive_scan_static_max())
+    g = torch.Generator(device="cuda").manual_seed(9)
+    full = torch.randint(0, 300, (limit,), dtype=torch.int32, device="cuda", generator=g)
+    a = static_scan(lib, full)
+    torch.cuda.synchronize()
+    assert torch.equal(a, allocating_scan(lib, full))
+    empty = torch.zeros(0, dtype=torch.int32, device="cuda")
+    z = static_scan(lib, empty)
+    torch.cuda.synchronize()
+    assert z.tolist() == [0]
+
+
 def test_static_scan_rejects_oversized_input():
     from diver_gb300 import _native
 
