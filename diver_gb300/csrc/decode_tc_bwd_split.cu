@@ -16,17 +16,19 @@
 // The forward is not recomputed: dv_decode_fwd_tc_split saved, per tile of 128
 // segments, every layer's input as two BF16 terms (X0, A1, A2, hidden, A4;
 // 16 KiB each), and its FP32 out4 gives the colour logits' sigmoid.  The
-// record is read into shared memory by bulk async copies.
+// record is read into shared memory by bulk async copies, one per layer slot.
 //
-// One CTA = 256 threads over one tile of 128 segments: thread t owns segment
-// row r = t % 128 (TMEM lane r; warps w and w + 4 share a lane quadrant) and
-// half h = t / 128 of each row's columns in the epilogues.  Shared memory
-// (about 162 KiB, one CTA per SM): transposed weight images in three terms,
-// the saved record, the PE tile in two terms, and the delta tile in three
-// terms (48 columns: the widest propagation K).  The weight-gradient MMA reads
-// the delta tile transposed with M = 128 output rows; rows past a layer's
-// outputs read the neighbouring (finite) data of the tile and of the next
-// term and land in TMEM rows that are never read.
+// One CTA per SM, 384 threads in two groups (see the kernel): 256 chain
+// threads, where thread t owns segment row r = t % 128 (TMEM lane r; warps w
+// and w + 4 share a lane quadrant) and half h = t / 128 of each row's columns
+// in the epilogues, and 128 scatter threads.  Shared memory (about 180 KiB):
+// transposed weight images in three terms, the saved record in five per-layer
+// slots, the PE tile in two terms, the delta tile in three terms (48 columns:
+// the widest propagation K) and the FP32 staging rows of the feature
+// gradient.  The weight-gradient MMA reads the delta tile transposed with
+// M = 128 output rows; rows past a layer's outputs read the neighbouring
+// (finite) data of the tile and of the next term and land in TMEM rows that
+// are never read.
 // Reference semantics: the autograd backward of model/diver.py:159-180.
 #include "common.cuh"
 #include "integrate.cuh"
@@ -40,7 +42,8 @@ namespace bws {
 
 constexpr int C = 32, W = 32;
 constexpr int NL = 5;
-constexpr int THREADS = 256;
+constexpr int CHAIN = 256;             // threads of the layer chain (warps 0-7)
+constexpr int THREADS = CHAIN + 128;   // + one warpgroup for the corner scatter
 constexpr int FD = 48;              // delta tile columns (K of the widest propagation MMA)
 constexpr int TILE = 128 * 32 * 2;  // one term of a [128][32] BF16 tile
 constexpr int DTILE = 128 * FD * 2; // one term of the delta tile
@@ -75,17 +78,19 @@ struct Args {
 
 // Shared-memory layout (byte offsets; wterm = 10240 for DIVeR32).
 struct Layout {
-  uint32_t bb, rec, pe, d, bar;
+  uint32_t bb, rec, pe, d, stage, bar;
   __host__ __device__ static Layout make(int wterm) {
     Layout L;
     L.bb = 0;
     L.rec = (uint32_t)(3 * wterm + 1023) / 1024 * 1024;
     L.pe = L.rec + RECORD;
     L.d = L.pe + 2 * TILE;
-    L.bar = L.d + 3 * DTILE;
+    L.stage = L.d + 3 * DTILE;
+    L.bar = L.stage + 128 * (C + 4) * 4;
     return L;
   }
-  __host__ __device__ uint32_t bytes() const { return bar + 32; }
+  // barriers: MMA completion, NL record slots; then the TMEM address and the abort flag
+  __host__ __device__ uint32_t bytes() const { return bar + 8 * (1 + NL) + 16; }
 };
 
 // Writes n values (multiple of 8) of row r, starting at column c0, as three
@@ -167,12 +172,6 @@ __device__ __forceinline__ void mma_dw(uint32_t tmem, const uint8_t* D, const ui
   }
 }
 
-__device__ __forceinline__ void sync_mma() {
-  tc::fence_before_sync();
-  tc::fence_async_smem();
-  __syncthreads();
-}
-
 // Rows [64 h, 64 h + 64) of column c of the two-term delta tile, summed.
 __device__ __forceinline__ float column_sum(const uint8_t* D, int c, int h) {
   float s = 0.f;
@@ -186,6 +185,66 @@ __device__ __forceinline__ float column_sum(const uint8_t* D, int c, int h) {
   return s;
 }
 
+// Named barriers of the two thread groups (barrier 0 is __syncthreads).
+constexpr int BAR_CHAIN = 1;       // the 256 chain threads among themselves
+constexpr int BAR_STAGE_FULL = 2;  // chain -> scatter: a tile's feature gradients are staged
+constexpr int BAR_STAGE_FREE = 3;  // scatter -> chain: the staging rows may be overwritten
+
+__device__ __forceinline__ void named_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void named_arrive(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+// AND of `v` over the n threads of named barrier `id` (all of them wait).
+__device__ __forceinline__ bool named_and(int id, int n, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, %2, %3, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(n)
+      : "memory");
+  return r != 0;
+}
+
+// Chain-group barrier that also orders generic-proxy shared-memory writes
+// before the tensor core's reads (and tcgen05 work across the barrier).
+__device__ __forceinline__ void chain_sync() {
+  tc::fence_before_sync();
+  tc::fence_async_smem();
+  named_sync(BAR_CHAIN, CHAIN);
+}
+
+// PE tile row r, columns 16h..16h+15 (PE_DIM = 27 values, zeros after), two terms.
+__device__ __forceinline__ void write_pe(const Args& a, uint8_t* PE, int ray, int r, int h) {
+  float v[16];
+  const float* pf = a.pe_feat + (long long)ray * PE_PAD + 16 * h;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = (16 * h + i < PE_DIM) ? __ldg(pf + i) : 0.f;
+  put2(PE, TILE, 32, r, 16 * h, v, 16);
+}
+
+// Delta of the colour logits (dL/drgb * sigmoid') into columns 0..15 of row r.
+__device__ __forceinline__ void write_delta4(uint8_t* D, int r, float4 g, float4 oc) {
+  float v[16];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = 0.f;
+  v[0] = g.y * oc.y * (1.f - oc.y);
+  v[1] = g.z * oc.z * (1.f - oc.z);
+  v[2] = g.w * oc.w * (1.f - oc.w);
+  put3(D, DTILE, FD, r, 0, v, 16);
+}
+
+// One tile per step of the persistent loop, in two concurrent groups:
+//   chain   (warps 0-7)  the five layer steps: per layer, the propagation and
+//                        weight-gradient MMAs, the bias column sums and the
+//                        epilogue that forms the next delta; it stages the
+//                        tile's feature gradient (FP32) for the scatter group
+//   scatter (warps 8-11) the previous tile's feature gradient into the 8
+//                        corner rows of every segment (vector atomics)
+// The saved record sits in five per-layer slots, each with its own mbarrier:
+// when a layer step of tile i is done with its slot, that slot is refilled
+// with tile i + gridDim.x's layer input, so the next tile's loads run behind
+// the rest of this tile.  The PE tile and the first delta of the next tile are
+// also written as soon as this tile is done with them.
 __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   const Layout lay = Layout::make(a.wterm);
@@ -193,129 +252,47 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
   uint8_t* REC = smem + lay.rec;
   uint8_t* PE = smem + lay.pe;
   uint8_t* D = smem + lay.d;
+  float* stage = reinterpret_cast<float*>(smem + lay.stage);  // [128][C + 4] FP32
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.bar);
-  uint64_t* bar_load = bar + 1;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
-  float* stage = reinterpret_cast<float*>(REC);  // [128][C + 4] FP32, once the record is consumed
+  uint64_t* bar_rec = bar + 1;  // [NL]: completion of slot l's record load
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1 + NL);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
 
-  const int t = threadIdx.x, warp = t >> 5, r = t & 127, h = t >> 7;
+  const int t = threadIdx.x, warp = t >> 5;
+  const bool chain = t < CHAIN;
+  const int r = t & 127, h = (t >> 7) & 1;
+  const long long S = segment_total(a.S, a.S_dev);
+  const long long tiles = (S + 127) / 128;
+
   for (int i = t; i < 3 * a.wterm / 16; i += THREADS)
     reinterpret_cast<uint4*>(Bb)[i] = __ldg(reinterpret_cast<const uint4*>(a.wb) + i);
   for (int i = t; i < 3 * DTILE / 16; i += THREADS) reinterpret_cast<uint4*>(D)[i] = make_uint4(0, 0, 0, 0);
   if (t == 0) {
     tc::mbar_init(bar, 1);
-    tc::mbar_init(bar_load, 1);
+    for (int l = 0; l < NL; ++l) tc::mbar_init(bar_rec + l, 1);
+    *abort_flag = 0;
     tc::fence_mbar_init();
   }
   if (warp == 0) {
     tc::tmem_alloc(tslot, TMEM_COLS);
     tc::tmem_relinquish();
   }
-  sync_mma();
+  tc::fence_before_sync();
+  tc::fence_async_smem();
+  __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
-  const uint32_t trow = tmem + lane;
-  uint32_t phase = 0, phase_load = 0;
-  bool ok = true, first = true;
-  float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  float v[32];
 
-  const long long S = segment_total(a.S, a.S_dev);
-  const long long tiles = (S + 127) / 128;
-  for (long long tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
-    const long long s = tile * 128 + r;
-    const bool valid = s < S;
-    sync_mma();  // the previous tile is done with the record, the staging alias, PE and D
-    if (t == 0) {
-      const uint8_t* rec = a.saved + tile * (long long)RECORD;
-      tc::mbar_arrive_expect_tx(bar_load, RECORD);
-      for (int l = 0; l < NL; ++l) tc::bulk_load(REC + l * 2 * TILE, rec + l * 2 * TILE, 2 * TILE, bar_load);
-    }
-    // PE tile (columns 16h..16h+15 of row r; PE_DIM = 27 values, zeros after)
-    const int ray = valid ? __ldg(a.seg_ray + s) : 0;
-    {
-      const float* pf = a.pe_feat + (long long)ray * PE_PAD + 16 * h;
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = (16 * h + i < PE_DIM) ? __ldg(pf + i) : 0.f;
-      put2(PE, TILE, 32, r, 16 * h, v, 16);
-    }
-    // delta of the colour logits: dL/drgb * sigmoid'
-    const float4 g = valid ? a.d4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (h == 0) {
-      const float4 oc = valid ? a.out4[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) v[i] = 0.f;
-      v[0] = g.y * oc.y * (1.f - oc.y);
-      v[1] = g.z * oc.z * (1.f - oc.z);
-      v[2] = g.w * oc.w * (1.f - oc.w);
-      put3(D, DTILE, FD, r, 0, v, 16);
-    }
-    ok = __syncthreads_and(tc::mbar_wait_bounded(bar_load, phase_load));
-    phase_load ^= 1u;
-    if (!ok) break;
-    sync_mma();
-
-    // layers last to first (unrolled: every layer constant is a compile-time value)
-#pragma unroll
-    for (int l = NL - 1; l >= 0; --l) {
-      const uint8_t* act = REC + l * 2 * TILE;  // this layer's input, two terms TILE apart
-      if (t == 0) {
-        tc::fence_after_sync();
-        mma_prop(tmem, D, Bb + a.b_img[l], a.wterm, KPROP(l), l == 0 ? C : W);
-        if (l == 3) {
-          mma_dw(tmem + DWCOL(3), D, act, !first);
-          mma_dw(tmem + DWCOL(3) + 32, D, PE, !first);
-        } else {
-          mma_dw(tmem + DWCOL(l), D, act, !first);
-        }
-        tc::mma_commit(bar);
-      }
-      if (r < OUT(l)) bias_acc[l] += column_sum(D, r, h);
-      const bool done = tc::mbar_wait_bounded(bar, phase);
-      phase ^= 1u;
-      tc::fence_after_sync();
-      ok = __syncthreads_and(done);  // also: every column sum is done before D is rewritten
-      if (!ok) break;
-      if (l == 3) {
-        // delta of layer 2: (dL/dsigma, d hidden[0..31]) in columns 0..32, zeros to 47;
-        // half 0 writes columns 0..23, half 1 columns 24..47
-        tc::ld_32x32b_x32(trow, v);
-        tc::ld_wait();
-        float w[24];
-        if (h == 0) {
-          w[0] = g.x;
-#pragma unroll
-          for (int i = 1; i < 24; ++i) w[i] = v[i - 1];
-        } else {
-#pragma unroll
-          for (int i = 0; i < 24; ++i) w[i] = (i + 23 < W) ? v[i + 23] : 0.f;
-        }
-        put3(D, DTILE, FD, r, 24 * h, w, 24);
-      } else if (l > 0) {
-        tc::ld_32x32b_x16(trow + 16 * h, v);
-        tc::ld_wait();
-        relu_mask(act, r, 16 * h, v, 16);  // this layer's input is relu of the previous layer's output
-        put3(D, DTILE, FD, r, 16 * h, v, 16);
-      } else {
-        // dL/dfeature, FP32, to the staging rows (the record is consumed)
-        tc::ld_32x32b_x16(trow + 16 * h, v);
-        tc::ld_wait();
-        float* st = stage + r * (C + 4) + 16 * h;
-#pragma unroll
-        for (int i = 0; i < 16; i += 4)
-          *reinterpret_cast<float4*>(st + i) =
-              valid ? make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]) : make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      sync_mma();
-    }
-    if (!ok) break;
-    first = false;
-    // ---- scatter dL/dfeature into the corner rows ----
-    {
-      constexpr int TPS = C / 4;
+  if (!chain) {
+    // ---------------- scatter group ----------------
+    const int u = t - CHAIN;  // 0..127
+    constexpr int TPS = C / 4;
+    if (blockIdx.x < tiles) named_arrive(BAR_STAGE_FREE, THREADS);  // the staging rows start free
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+      named_sync(BAR_STAGE_FULL, THREADS);
+      if (*reinterpret_cast<volatile int*>(abort_flag)) break;
 #pragma unroll 1
-      for (int i = t; i < 128 * TPS; i += THREADS) {
+      for (int i = u; i < 128 * TPS; i += 128) {
         const int ls = i / TPS, q = i % TPS;
         const long long ss = tile * 128 + ls;
         if (ss < S) {
@@ -326,27 +303,167 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
           scatter4(a.grad_grid, sc, C, q, gf, a.nvx, a.nvy);
         }
       }
+      __threadfence_block();
+      if (tile + gridDim.x < tiles) named_arrive(BAR_STAGE_FREE, THREADS);
     }
-  }
-  if (!ok && t == 0 && a.err) atomicExch(a.err, 1);
-  // ---- flush: weight gradients from TMEM (row o = out index = this thread's lane) ----
-  if (ok && !first) {
+  } else {
+    // ---------------- chain group ----------------
+    const uint32_t lane = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t trow = tmem + lane;
+    uint32_t phase = 0, phase_rec = 0;  // phase_rec: bit l = parity of slot l's next completion
+    uint32_t pending = 0;               // thread 0: slots with a load in flight
+    bool mma_inflight = false;          // thread 0: an MMA batch committed and not yet waited for
+    bool ok = true, first = true;
+    float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    float v[32];
+    // the CTA's first tile: record loads, PE tile, first delta
+    long long tile = blockIdx.x;
+    if (tile < tiles) {
+      if (t == 0) {
+        const uint8_t* rec = a.saved + tile * (long long)RECORD;
+        for (int l = 0; l < NL; ++l) {
+          tc::mbar_arrive_expect_tx(bar_rec + l, 2 * TILE);
+          tc::bulk_load(REC + l * 2 * TILE, rec + l * 2 * TILE, 2 * TILE, bar_rec + l);
+        }
+        pending = (1u << NL) - 1;
+      }
+      const long long s = tile * 128 + r;
+      const bool valid = s < S;
+      write_pe(a, PE, valid ? __ldg(a.seg_ray + s) : 0, r, h);
+      if (h == 0)
+        write_delta4(D, r, valid ? a.d4[s] : make_float4(0.f, 0.f, 0.f, 0.f),
+                     valid ? a.out4[s] : make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+    for (; tile < tiles && ok; tile += gridDim.x) {
+      const long long s = tile * 128 + r;
+      const bool valid = s < S;
+      const long long next = tile + gridDim.x;
+      const long long sn = next * 128 + r;
+      const bool valid_next = next < tiles && sn < S;
+      const float gx = valid ? a.d4[s].x : 0.f;  // dL/dsigma of this row (layer 2's delta)
+      chain_sync();  // the PE tile and the first delta are in place
+      // layers last to first (unrolled: every layer constant is a compile-time value)
 #pragma unroll
-    for (int l = 0; l < NL; ++l) {
-      const int o = r;
-#pragma unroll
-      for (int c0 = 0; c0 < NIN(l); c0 += 32) {
-        tc::ld_32x32b_x16(tmem + lane + DWCOL(l) + c0 + 16 * h, v);
-        tc::ld_wait();
-        if (o < OUT(l)) {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int c = c0 + 16 * h + i;
-            if (c < IN(l)) atomicAdd(a.grad_params + a.w_off[l] + c * OUT4(l) + o, v[i]);
+      for (int l = NL - 1; l >= 0; --l) {
+        const uint8_t* act = REC + l * 2 * TILE;  // this layer's input, two terms TILE apart
+        // this layer's record slot has arrived (bounded wait; the parities
+        // advance only on success: after a timeout the abort path waits with them)
+        const bool arrived = tc::mbar_wait_bounded(bar_rec + l, (phase_rec >> l) & 1u);
+        if (arrived) phase_rec ^= 1u << l;
+        if (t == 0 && arrived) {
+          pending &= ~(1u << l);
+          tc::fence_after_sync();
+          mma_prop(tmem, D, Bb + a.b_img[l], a.wterm, KPROP(l), l == 0 ? C : W);
+          if (l == 3) {
+            mma_dw(tmem + DWCOL(3), D, act, !first);
+            mma_dw(tmem + DWCOL(3) + 32, D, PE, !first);
+          } else {
+            mma_dw(tmem + DWCOL(l), D, act, !first);
+          }
+          tc::mma_commit(bar);
+          mma_inflight = true;
+        }
+        if (r < OUT(l)) bias_acc[l] += column_sum(D, r, h);
+        // thread 0 issued nothing if its slot wait gave up: the AND below then stops every thread
+        const bool issued = named_and(BAR_CHAIN, CHAIN, arrived);
+        bool done = false;
+        if (issued) {
+          done = tc::mbar_wait_bounded(bar, phase);
+          if (done) {
+            phase ^= 1u;
+            mma_inflight = false;
           }
         }
+        tc::fence_after_sync();
+        ok = named_and(BAR_CHAIN, CHAIN, issued && done);  // also: every column sum is done before D is rewritten
+        if (!ok) break;
+        if (l == 3) {
+          // delta of layer 2: (dL/dsigma, d hidden[0..31]) in columns 0..32, zeros to 47;
+          // half 0 writes columns 0..23, half 1 columns 24..47
+          tc::ld_32x32b_x32(trow, v);
+          tc::ld_wait();
+          float w[24];
+          if (h == 0) {
+            w[0] = gx;
+#pragma unroll
+            for (int i = 1; i < 24; ++i) w[i] = v[i - 1];
+          } else {
+#pragma unroll
+            for (int i = 0; i < 24; ++i) w[i] = (i + 23 < W) ? v[i + 23] : 0.f;
+          }
+          put3(D, DTILE, FD, r, 24 * h, w, 24);
+          // this tile's PE is consumed: the next tile's goes in now
+          if (next < tiles) write_pe(a, PE, valid_next ? __ldg(a.seg_ray + sn) : 0, r, h);
+        } else if (l > 0) {
+          tc::ld_32x32b_x16(trow + 16 * h, v);
+          tc::ld_wait();
+          relu_mask(act, r, 16 * h, v, 16);  // this layer's input is relu of the previous layer's output
+          put3(D, DTILE, FD, r, 16 * h, v, 16);
+        } else {
+          // dL/dfeature (FP32) to the staging rows once the scatter group is done with them
+          float4 gn = make_float4(0.f, 0.f, 0.f, 0.f), on = gn;
+          if (valid_next && h == 0) {
+            gn = a.d4[sn];
+            on = a.out4[sn];
+          }
+          tc::ld_32x32b_x16(trow + 16 * h, v);
+          tc::ld_wait();
+          named_sync(BAR_STAGE_FREE, THREADS);
+          float* st = stage + r * (C + 4) + 16 * h;
+#pragma unroll
+          for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4*>(st + i) =
+                valid ? make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]) : make_float4(0.f, 0.f, 0.f, 0.f);
+          __threadfence_block();
+          named_arrive(BAR_STAGE_FULL, THREADS);
+          // this tile's deltas are consumed: the next tile's first delta goes in now
+          if (next < tiles && h == 0) write_delta4(D, r, gn, on);
+        }
+        chain_sync();  // D is complete for the next layer; every read of this layer's slot is done
+        if (t == 0 && next < tiles) {
+          // refill this layer's slot with the next tile's input
+          tc::mbar_arrive_expect_tx(bar_rec + l, 2 * TILE);
+          tc::bulk_load(REC + l * 2 * TILE, a.saved + next * (long long)RECORD + l * 2 * TILE, 2 * TILE,
+                        bar_rec + l);
+          pending |= 1u << l;
+        }
       }
-      if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, bias_acc[l]);
+      if (!ok) break;
+      first = false;
+    }
+    if (!ok) {
+      if (t == 0) {
+        if (a.err) atomicExch(a.err, 1);
+        *reinterpret_cast<volatile int*>(abort_flag) = 1;
+        // record loads and MMAs still in flight complete before the CTA frees
+        // its shared memory and TMEM (bounded waits)
+        for (int l = 0; l < NL; ++l)
+          if ((pending >> l) & 1u) tc::mbar_wait_bounded(bar_rec + l, (phase_rec >> l) & 1u);
+        if (mma_inflight) tc::mbar_wait_bounded(bar, phase);
+      }
+      __threadfence_block();
+      named_sync(BAR_CHAIN, CHAIN);
+      named_arrive(BAR_STAGE_FULL, THREADS);  // wakes the scatter group, which sees the flag and stops
+    }
+    // ---- flush: weight gradients from TMEM (row o = out index = this thread's lane) ----
+    if (ok && !first) {
+#pragma unroll
+      for (int l = 0; l < NL; ++l) {
+        const int o = r;
+#pragma unroll
+        for (int c0 = 0; c0 < NIN(l); c0 += 32) {
+          tc::ld_32x32b_x16(tmem + lane + DWCOL(l) + c0 + 16 * h, v);
+          tc::ld_wait();
+          if (o < OUT(l)) {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              const int c = c0 + 16 * h + i;
+              if (c < IN(l)) atomicAdd(a.grad_params + a.w_off[l] + c * OUT4(l) + o, v[i]);
+            }
+          }
+        }
+        if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, bias_acc[l]);
+      }
     }
   }
   tc::fence_before_sync();
