@@ -6,7 +6,8 @@
 //     each, the six products whose term indices add up to at most 2;
 //   - weight gradient    dW += delta^T @ activation: two terms each, three
 //     products (FP32 accumulators resident in TMEM for the CTA's life);
-//   - bias gradient      column sums of the two-term delta (CUDA cores).
+//   - bias gradient      dB += delta^T @ ones: the column sums of the two-term
+//     delta as two more products per layer, also accumulated in TMEM.
 // Products are accumulated in FP32 in TMEM, so the propagated deltas and the
 // gradients keep about 2^-24 (propagation) and 2^-16 (weight gradients) of
 // relative precision per product; emulating the kernel's arithmetic on the
@@ -21,11 +22,11 @@
 // One CTA per SM, 384 threads in two groups (see the kernel): 256 chain
 // threads, where thread t owns segment row r = t % 128 (TMEM lane r; warps w
 // and w + 4 share a lane quadrant) and half h = t / 128 of each row's columns
-// in the epilogues, and 128 scatter threads.  Shared memory (about 180 KiB):
+// in the epilogues, and 128 scatter threads.  Shared memory (about 184 KiB):
 // transposed weight images in three terms, the saved record in five per-layer
 // slots, the PE tile in two terms, the delta tile in three terms (48 columns:
-// the widest propagation K) and the FP32 staging rows of the feature
-// gradient.  The weight-gradient MMA reads the delta tile transposed with
+// the widest propagation K), a tile of ones and the FP32 staging rows of the
+// feature gradient.  TMEM: all 512 columns (working, weight and bias gradients).  The weight-gradient MMA reads the delta tile transposed with
 // M = 128 output rows; rows past a layer's outputs read the neighbouring
 // (finite) data of the tile and of the next term and land in TMEM rows that
 // are never read.
@@ -47,15 +48,17 @@ constexpr int THREADS = CHAIN + 128;   // + one warpgroup for the corner scatter
 constexpr int FD = 48;              // delta tile columns (K of the widest propagation MMA)
 constexpr int TILE = 128 * 32 * 2;  // one term of a [128][32] BF16 tile
 constexpr int DTILE = 128 * FD * 2; // one term of the delta tile
-constexpr int TMEM_COLS = 256;
+constexpr int TMEM_COLS = 512;     // 64 working + 192 weight-gradient + 80 bias-gradient columns, rounded up
 // layer: 0 (C->W), 1 (W->W), 2 (W->W+1: sigma, hidden), 3 (W+27->W), 4 (W->3)
 __host__ __device__ constexpr int IN(int l) { return l == 0 ? C : (l == 3 ? W + PE_DIM : W); }
 __host__ __device__ constexpr int OUT(int l) { return l == 2 ? W + 1 : (l == 4 ? 3 : W); }
 __host__ __device__ constexpr int OUT4(int l) { return pad4(OUT(l)); }
 __host__ __device__ constexpr int NIN(int l) { return l == 3 ? 64 : 32; }  // weight-gradient columns (in, padded)
 __host__ __device__ constexpr int DWCOL(int l) { return l == 0 ? 64 : (l <= 3 ? DWCOL(l - 1) + NIN(l - 1) : 224); }
+__host__ __device__ constexpr int DBCOL(int l) { return 256 + 16 * l; }  // bias gradient of layer l (column 0 of 16)
 __host__ __device__ constexpr int KPROP(int l) { return l == 4 ? 16 : (l == 2 ? W + 16 : W); }  // propagation K
 constexpr uint32_t RECORD = 5 * 2 * TILE;  // saved record of one tile: 5 layer inputs x 2 terms
+constexpr uint32_t ONES_BYTES = 128 * 16 * 2;  // a [128][16] BF16 tile of ones
 
 struct Args {
   int nvx, nvy, nvz;
@@ -78,14 +81,15 @@ struct Args {
 
 // Shared-memory layout (byte offsets; wterm = 10240 for DIVeR32).
 struct Layout {
-  uint32_t bb, rec, pe, d, stage, bar;
+  uint32_t bb, rec, pe, d, ones, stage, bar;
   __host__ __device__ static Layout make(int wterm) {
     Layout L;
     L.bb = 0;
     L.rec = (uint32_t)(3 * wterm + 1023) / 1024 * 1024;
     L.pe = L.rec + RECORD;
     L.d = L.pe + 2 * TILE;
-    L.stage = L.d + 3 * DTILE;
+    L.ones = L.d + 3 * DTILE;
+    L.stage = L.ones + ONES_BYTES;
     L.bar = L.stage + 128 * (C + 4) * 4;
     return L;
   }
@@ -172,17 +176,21 @@ __device__ __forceinline__ void mma_dw(uint32_t tmem, const uint8_t* D, const ui
   }
 }
 
-// Rows [64 h, 64 h + 64) of column c of the two-term delta tile, summed.
-__device__ __forceinline__ float column_sum(const uint8_t* D, int c, int h) {
-  float s = 0.f;
-#pragma unroll 8
-  for (int r = 64 * h; r < 64 * h + 64; ++r) {
-    const uint32_t off = tc::kmajor_offset(r, c, FD);
-    const uint16_t a = *reinterpret_cast<const uint16_t*>(D + off);
-    const uint16_t b = *reinterpret_cast<const uint16_t*>(D + DTILE + off);
-    s += __uint_as_float((uint32_t)a << 16) + __uint_as_float((uint32_t)b << 16);
+// Bias gradient over the tile's 128 segments: TMEM dB[128 = out][16] += delta^T x
+// ones, i.e. every column of dB is the column sum of the delta (two terms, two
+// products; the ones are exact in BF16).  The ones tile is all ones, so any
+// reading of its layout is the same.
+__device__ __forceinline__ void mma_db(uint32_t tmem, const uint8_t* D, const uint8_t* ones, bool accumulate) {
+  const uint32_t idesc = tc::idesc_f16(128, 16, 1) | (1u << 15) | (1u << 16);
+  constexpr uint32_t lboA = (FD / 8) * 128, lboB = (16 / 8) * 128;
+  const uint32_t b0 = tc::smem_u32(ones);
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const uint32_t a0 = tc::smem_u32(D + p * DTILE);
+    for (int k = 0; k < 8; ++k)
+      tc::mma_f16(tmem, tc::smem_desc(a0 + k * 2 * lboA, lboA, 128), tc::smem_desc(b0 + k * 2 * lboB, lboB, 128),
+                  idesc, (accumulate || p > 0 || k > 0) ? 1u : 0u);
   }
-  return s;
 }
 
 // Named barriers of the two thread groups (barrier 0 is __syncthreads).
@@ -252,6 +260,7 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
   uint8_t* REC = smem + lay.rec;
   uint8_t* PE = smem + lay.pe;
   uint8_t* D = smem + lay.d;
+  uint8_t* ONES = smem + lay.ones;
   float* stage = reinterpret_cast<float*>(smem + lay.stage);  // [128][C + 4] FP32
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + lay.bar);
   uint64_t* bar_rec = bar + 1;  // [NL]: completion of slot l's record load
@@ -267,6 +276,8 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
   for (int i = t; i < 3 * a.wterm / 16; i += THREADS)
     reinterpret_cast<uint4*>(Bb)[i] = __ldg(reinterpret_cast<const uint4*>(a.wb) + i);
   for (int i = t; i < 3 * DTILE / 16; i += THREADS) reinterpret_cast<uint4*>(D)[i] = make_uint4(0, 0, 0, 0);
+  for (int i = t; i < (int)ONES_BYTES / 16; i += THREADS)
+    reinterpret_cast<uint4*>(ONES)[i] = make_uint4(0x3f803f80u, 0x3f803f80u, 0x3f803f80u, 0x3f803f80u);  // bf16 1.0
   if (t == 0) {
     tc::mbar_init(bar, 1);
     for (int l = 0; l < NL; ++l) tc::mbar_init(bar_rec + l, 1);
@@ -314,7 +325,6 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
     uint32_t pending = 0;               // thread 0: slots with a load in flight
     bool mma_inflight = false;          // thread 0: an MMA batch committed and not yet waited for
     bool ok = true, first = true;
-    float bias_acc[NL] = {0.f, 0.f, 0.f, 0.f, 0.f};
     float v[32];
     // the CTA's first tile: record loads, PE tile, first delta
     long long tile = blockIdx.x;
@@ -360,22 +370,22 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
           } else {
             mma_dw(tmem + DWCOL(l), D, act, !first);
           }
+          mma_db(tmem + DBCOL(l), D, ONES, !first);
           tc::mma_commit(bar);
           mma_inflight = true;
         }
-        if (r < OUT(l)) bias_acc[l] += column_sum(D, r, h);
-        // thread 0 issued nothing if its slot wait gave up: the AND below then stops every thread
-        const bool issued = named_and(BAR_CHAIN, CHAIN, arrived);
+        // if thread 0's slot wait gave up it issued nothing: every thread's MMA wait then
+        // runs out too, and the AND below stops them all
         bool done = false;
-        if (issued) {
+        if (arrived) {
           done = tc::mbar_wait_bounded(bar, phase);
           if (done) {
             phase ^= 1u;
-            mma_inflight = false;
+            if (t == 0) mma_inflight = false;
           }
         }
         tc::fence_after_sync();
-        ok = named_and(BAR_CHAIN, CHAIN, issued && done);  // also: every column sum is done before D is rewritten
+        ok = named_and(BAR_CHAIN, CHAIN, arrived && done);
         if (!ok) break;
         if (l == 3) {
           // delta of layer 2: (dL/dsigma, d hidden[0..31]) in columns 0..32, zeros to 47;
@@ -462,7 +472,11 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
             }
           }
         }
-        if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, bias_acc[l]);
+        if (h == 0) {
+          tc::ld_32x32b_x16(tmem + lane + DBCOL(l), v);
+          tc::ld_wait();
+          if (o < OUT(l)) atomicAdd(a.grad_params + a.b_off[l] + o, v[0]);
+        }
       }
     }
   }
