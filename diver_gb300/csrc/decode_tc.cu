@@ -88,6 +88,53 @@ __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, lon
   }
 }
 
+// The split form's gather (FP32 grid, three operand terms): the same passes as
+// gather_tile_lp, two at a time, so each thread has 16 corner-row loads in
+// flight.  The split kernel runs 4 CTAs per SM (its shared memory), so the
+// registers this takes cost no residency; the single-term kernels keep the
+// one-pass gather (their residency is register-bound).
+template <int C, int TERMS>
+__device__ __forceinline__ void gather_tile_lp_x2(const TcArgs& a, long long S, long long s0, uint8_t* sA,
+                                                  uint32_t tstride) {
+  constexpr int TPS = C / 4;
+  constexpr int SPP = 128 / TPS;
+  static_assert(TPS % 2 == 0, "passes are taken in pairs");
+  const int t = threadIdx.x;
+  const int q = t % TPS;
+#pragma unroll 1
+  for (int p = 0; p < TPS; p += 2) {
+    SegCorner sc[2];
+    float4 v[2][8];
+    bool in[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const long long s = s0 + (p + u) * SPP + t / TPS;
+      in[u] = s < S;
+      if (in[u]) {
+        const float* sg = a.seg + s * 6;
+        sc[u] = segment_corners(__ldg(sg), __ldg(sg + 1), __ldg(sg + 2), __ldg(sg + 3), __ldg(sg + 4), __ldg(sg + 5),
+                                a.nvx, a.nvy, a.nvz);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[u][j] = ldg4(a.grid + corner_row(sc[u], j, a.nvx, a.nvy) * C + q * 4);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in[u]) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) fma4(f, sc[u].w[j], v[u][j]);
+      }
+      uint32_t x[TERMS], y[TERMS];
+      tc::split_pair<TERMS>(f.x, f.y, x);
+      tc::split_pair<TERMS>(f.z, f.w, y);
+      uint8_t* dst = sA + tc::kmajor_offset((p + u) * SPP + t / TPS, 4 * q, C);
+#pragma unroll
+      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint2*>(dst + i * tstride) = make_uint2(x[i], y[i]);
+    }
+  }
+}
+
 template <int BF16>
 __device__ __forceinline__ void unpack8(const uint4 w, float* f) {
   const uint32_t x[4] = {w.x, w.y, w.z, w.w};
@@ -216,8 +263,11 @@ __device__ __forceinline__ void sync_for_mma() {
 // NCOLS: TMEM columns (>= widest N, power of two >= 32).  TERMS: operand
 // terms (1: BF16 or FP16 operands; 3: FP32 values as three BF16 terms, six
 // products per layer, FP32-grade; BF16 only and read from the FP32 grid).
+// Registers per thread are capped to the residency the other resources allow:
+// 8 CTAs per SM for the single-term forms (TMEM), 4 for the DIVeR32 split
+// form (shared memory; its two-pass gather would otherwise take 3).
 template <int C, int W, int D1, int BF16, int NCOLS, int TERMS>
-__global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
+__global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 4 : 1)) decode_fwd_tc(const TcArgs a) {
   constexpr int KMAX = C > W ? C : W;
   constexpr uint32_t TSTRIDE = 128 * KMAX * 2;  // bytes between the A tile's terms
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -253,10 +303,14 @@ __global__ void __launch_bounds__(128) decode_fwd_tc(const TcArgs a) {
     const bool valid = s < S;
     uint8_t* rec = a.save ? a.save + tile * (long long)a.save_bytes : nullptr;
 #define DV_SAVE(l) (rec ? rec + a.save_off[l] : nullptr)
-    if (TERMS == 1 && a.grid16)
-      gather_tile_16<C, BF16>(a, S, s0, sA);
-    else
-      gather_tile_lp<C, BF16, TERMS>(a, S, s0, sA, TSTRIDE);
+    if constexpr (TERMS > 1) {
+      gather_tile_lp_x2<C, TERMS>(a, S, s0, sA, TSTRIDE);
+    } else {
+      if (a.grid16)
+        gather_tile_16<C, BF16>(a, S, s0, sA);
+      else
+        gather_tile_lp<C, BF16, TERMS>(a, S, s0, sA, TSTRIDE);
+    }
     sync_for_mma();
     float v[32];
     // mlp1 hidden layers: D = relu(A W^T + b)
