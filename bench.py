@@ -658,16 +658,20 @@ def run_realtime(args, dev):
     rounds = []
 
     def frame_loop(i):
-        _, r = model.render_frame(*frames[i % 100], fused=False)
+        _, r = model.render_frame(*frames[i % 100], mode="loop")
         rounds.append(r)
 
     loop = _frame_times(frame_loop, 10, 1)
-    fused = _frame_times(lambda i: model.render_frame(*frames[i % 100]), 100, 3)
-    p50 = statistics.median(fused)
-    return {"frame_ms": p50, "p50_ms": p50, "p99_ms": pct(fused, 0.99), "frames": len(fused),
-            "Mrays_per_s": 640000 / (p50 * 1e-3) / 1e6, "form": "one launch per frame",
+    fused = _frame_times(lambda i: model.render_frame(*frames[i % 100], mode="fused"), 100, 3)
+    tc = _frame_times(lambda i: model.render_frame(*frames[i % 100], mode="tc"), 100, 3)
+    p50 = statistics.median(tc)
+    return {"frame_ms": p50, "p50_ms": p50, "p99_ms": pct(tc, 0.99), "frames": len(tc),
+            "Mrays_per_s": 640000 / (p50 * 1e-3) / 1e6,
+            "form": "aabb_intersect + rounds of ray_march and the tcgen05 decoder (split BF16 operands, FP32-grade)",
+            "fused_fp32": {"p50_ms": statistics.median(fused), "p99_ms": pct(fused, 0.99), "frames": len(fused),
+                           "form": "one launch per frame, FP32 decoder"},
             "host_loop": {"frame_ms": statistics.median(loop), "frames": len(loop), "rounds": rounds[-1],
-                          "form": "aabb_intersect + rounds of ray_march / mlp_eval (the reference's loop)"},
+                          "form": "aabb_intersect + rounds of ray_march / mlp_eval (the reference's loop, FP32 decoder)"},
             "features": int(ser["f"].shape[0])}
 
 

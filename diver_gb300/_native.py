@@ -69,6 +69,9 @@ SIGNATURES = {
     "dv_realtime_packed_size": (I32, [I32]),
     "dv_realtime_pack": (I32, [I32, P, P, P]),
     "dv_mlp_eval": (I32, [I32, I32, P, P, P, I32, P, P, P, P, P]),
+    "dv_realtime_tc_bytes": (I32, [I32]),
+    "dv_realtime_tc_pack": (I32, [I32, P, P, P]),
+    "dv_mlp_eval_tc": (I32, [I32, I32, P, P, P, I32, P, P, P, P, P, P, P]),
     "dv_realtime_frame": (I32, [I32, I32, P, P, P, I32, P, P, P, I32, P, P, P]),
     "dv_aabb_intersect": (I32, [I32, P, P, P, P, P, P, I32, P]),
     "dv_ray_march": (I32, [I32, P, P, P, P, I32, P]),

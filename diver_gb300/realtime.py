@@ -86,25 +86,55 @@ class RealtimeModel:
                              build_octree_levels(masks), RealtimeModel.pack_params(p, width, device), width,
                              voxel_num, xyzmin, voxel_size)
 
-    def mlp_eval(self, rgba, coords, v, finish):
+    def tc_blob(self) -> torch.Tensor:
+        """Tensor-core images of the folded layers (three BF16 terms), made once
+        per model from the aligned params on the device."""
+        blob = getattr(self, "_tc_blob", None)
+        if blob is None:
+            dev = self.packed.device
+            blob = torch.empty(N.lib().dv_realtime_tc_bytes(self.width), dtype=torch.uint8, device=dev)
+            N.call("dv_realtime_tc_pack", self.width, N.ptr(self.packed), N.ptr(blob), N.stream(dev))
+            self._tc_blob = blob
+            self.tc_err = torch.zeros(1, dtype=torch.int32, device=dev)
+        return blob
+
+    def mlp_eval(self, rgba, coords, v, finish, tensor_cores: bool = False):
+        """One round of the fused decoder on the recorded hits (mlp_eval.cu:32-231),
+        in place on rgba / finish; tensor_cores: the tcgen05 form (dv_mlp_eval_tc)."""
         fin = finish.view(torch.uint8) if finish.dtype == torch.bool else finish
         B = v.numel() // 3
+        if tensor_cores:
+            blob = self.tc_blob()
+            N.call("dv_mlp_eval_tc", self.width, B, N.ptr(coords), N.ptr(self.features), N.ptr(self.voxel_map),
+                   self.voxel_map.shape[0], N.ptr(self.packed), N.ptr(blob), N.ptr(v), N.ptr(rgba), N.ptr(fin),
+                   N.ptr(self.tc_err), N.stream(v.device))
+            return
         N.call("dv_mlp_eval", self.width, B, N.ptr(coords), N.ptr(self.features), N.ptr(self.voxel_map),
                self.voxel_map.shape[0], N.ptr(self.packed), N.ptr(v), N.ptr(rgba), N.ptr(fin), N.stream(v.device))
 
     def render_frame(self, eye: torch.Tensor, dirs: torch.Tensor, max_rounds: int | None = None,
-                     fused: bool = True):
+                     fused: bool | None = None, mode: str = "tc"):
         """rgb [B,3] of B rays from camera centre `eye` (world) with unit
         directions `dirs` [B,3] (eval_rt.py:106-122); also returns the number of
-        host rounds.  fused (default): the whole frame in one launch
-        (dv_realtime_frame, same result); otherwise the reference's loop of
-        aabb_intersect, then ray_march + mlp_eval rounds until every pixel is
-        finished (max_rounds caps it)."""
+        host rounds.  mode:
+          "tc"     (default) the reference's loop of aabb_intersect, then rounds
+                   of ray_march + the tensor-core decoder (dv_mlp_eval_tc,
+                   FP32-grade) until every pixel is finished
+          "fused"  the whole frame in one launch with the FP32 decoder
+                   (dv_realtime_frame)
+          "loop"   the reference's loop with the FP32 decoder (dv_mlp_eval);
+                   same result as "fused"
+        fused=True / False select "fused" / "loop" (the earlier form of this
+        argument); max_rounds caps the rounds of the loops."""
+        if fused is not None:
+            mode = "fused" if fused else "loop"
+        if mode not in ("tc", "fused", "loop"):
+            raise ValueError(f"unknown real-time frame mode {mode!r}")
         dev = dirs.device
         B = dirs.shape[0]
         v = dirs.contiguous()
         center = ((eye.float().cpu() - self.xyzmin) / self.voxel_size).to(dev).contiguous()
-        if fused:
+        if mode == "fused":
             rgba = torch.empty(B, 4, device=dev)
             m8 = self.voxel_masks.view(torch.uint8) if self.voxel_masks.dtype == torch.bool else self.voxel_masks
             o8 = self.octrees.view(torch.uint8) if self.octrees.dtype == torch.bool else self.octrees
@@ -120,7 +150,7 @@ class RealtimeModel:
         limit = max_rounds if max_rounds is not None else 3 * self.voxel_num
         while rounds < limit and not bool(finish.all()):
             ray_march(coords, v, self.voxel_masks, finish, self.voxel_num)
-            self.mlp_eval(rgba, coords, v, finish)
+            self.mlp_eval(rgba, coords, v, finish, mode == "tc")
             rounds += 1
         return rgba[:, :3] + rgba[:, 3:], rounds
 

@@ -479,6 +479,25 @@ DV_API int dv_mlp_eval(int width, int batch_size, const float* coords, const flo
                        float* rgba, uint8_t* finish, void* stream);
 
 /*
+ * Tensor-core form of dv_mlp_eval (same contract: rgba and finish in place,
+ * coords [8][B][6], the sparse feature table, the index map, the aligned
+ * params of dv_realtime_pack), replacing the per-pixel FP32 layer loops of the
+ * reference kernel (utils/mlp_evaluation{,64}/src/mlp_eval.cu:125-209) with
+ * tcgen05 MMAs over tiles of 128 pixels, one tile per hit slot.  Operands
+ * are split BF16 (three terms, six products per layer), so the results are
+ * FP32-grade.  tc_blob: dv_realtime_tc_bytes(width) bytes (16-byte aligned)
+ * filled once per model by dv_realtime_tc_pack from the same aligned params.
+ * err (device int, optional): set to 1 if a bounded MMA completion wait ran
+ * out.
+ */
+DV_API int dv_realtime_tc_bytes(int width);
+DV_API int dv_realtime_tc_pack(int width, const float* packed_params, void* tc_blob, void* stream);
+DV_API int dv_mlp_eval_tc(int width, int batch_size, const float* coords, const float* voxels,
+                          const int* voxel_map, int map_size, const float* packed_params,
+                          const void* tc_blob, const float* v, float* rgba, uint8_t* finish, int* err,
+                          void* stream);
+
+/*
  * Whole real-time frame in one launch (no counterpart call in the reference,
  * whose eval_rt.py:115-122 loops on the host: dv_aabb_intersect, then rounds
  * of dv_ray_march + dv_mlp_eval until every pixel is finished).  Per pixel:

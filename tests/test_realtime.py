@@ -70,8 +70,8 @@ def test_realtime_frame_matches_oracle_loop(kind, width):
     sc, ser, model = small_realtime(kind, "cuda")
     c2w = scenes.sphere_cameras(1, 4.0, 3)[0]
     o, v = scenes.camera_rays(c2w, 128, 128, 153.6, "cpu")
-    rgb, rounds = model.render_frame(c2w[:, 3], v.cuda(), fused=False)
-    rgb_fused, _ = model.render_frame(c2w[:, 3], v.cuda())
+    rgb, rounds = model.render_frame(c2w[:, 3], v.cuda(), mode="loop")
+    rgb_fused, _ = model.render_frame(c2w[:, 3], v.cuda(), mode="fused")
     # the single-launch frame performs the same per-pixel arithmetic as the loop
     assert torch.equal(rgb_fused, rgb)
     # oracle: same loop with the C restatements
@@ -109,12 +109,14 @@ MLP_EVAL_FLIPS = 2e-3
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tensor_cores", [False, True], ids=["fp32", "tcgen05"])
 @pytest.mark.parametrize("kind,width", [("diver32", 32), ("diver64", 64)])
-def test_realtime_decoder_matches_reference_kernel_outputs(kind, width, golden):
+def test_realtime_decoder_matches_reference_kernel_outputs(kind, width, tensor_cores, golden):
     """The real-time loop (octree first hit, rounds of 8-hit march + fused
     decoder) on rows 392..407 of an 800x800 view against the outputs of the
     reference's own mlp_eval kernels run on a GB300: rgba after the first
-    round and after the last, finish flags and round count."""
+    round and after the last, finish flags and round count; for the FP32
+    decoder (dv_mlp_eval) and the tensor-core one (dv_mlp_eval_tc)."""
     from diver_gb300 import scenes
     from diver_gb300.ray_march import aabb_intersect, ray_march
 
@@ -135,18 +137,41 @@ def test_realtime_decoder_matches_reference_kernel_outputs(kind, width, golden):
     first = None
     while not bool(finish.all()) and rounds < 3 * 64:
         ray_march(coords, v, model.voxel_masks, finish, 64)
-        model.mlp_eval(rgba, coords, v, finish)
+        model.mlp_eval(rgba, coords, v, finish, tensor_cores)
         rounds += 1
         if first is None:
             first = rgba.cpu().numpy().copy()
     got = rgba.cpu().numpy()
     for mine, ref in ((first, g[f"{kind}/rgba_round1"]), (got, g[f"{kind}/rgba"])):
         err = np.abs(mine - ref).max(1)
-        print(f"MLPEVALREF kind={kind} max_abs={err.max():.2e} p99.8={np.quantile(err, 0.998):.2e} "
+        print(f"MLPEVALREF kind={kind} tc={tensor_cores} max_abs={err.max():.2e} p99.8={np.quantile(err, 0.998):.2e} "
               f"over_tol={float((err > MLP_EVAL_TOL).mean()):.2e}")
         assert (err > MLP_EVAL_TOL).mean() <= MLP_EVAL_FLIPS, err.max()
     assert (finish.cpu().numpy().astype(bool) != g[f"{kind}/finish"].astype(bool)).mean() <= MLP_EVAL_FLIPS
     assert abs(rounds - int(g[f"{kind}/rounds"])) <= 1
-    # the one-launch frame gives the loop's result
-    rgb_fused, _ = model.render_frame(c2w[:, 3], v)
-    assert torch.equal(rgb_fused.cpu(), torch.from_numpy(got[:, :3] + got[:, 3:]))
+    if tensor_cores:
+        assert int(model.tc_err.item()) == 0
+    # the frame driver gives the loop's result (one launch for the FP32 decoder)
+    rgb_frame, _ = model.render_frame(c2w[:, 3], v, mode="tc" if tensor_cores else "fused")
+    assert torch.equal(rgb_frame.cpu(), torch.from_numpy(got[:, :3] + got[:, 3:]))
+
+
+@pytest.mark.gpu
+def test_tensor_core_frame_matches_fp32_frame_on_the_256_scene():
+    """Full 800x800 frame of the 256^3 DIVeR32 scene: the tensor-core decoder
+    against the FP32 one (same march), rgb within the fixture tolerance."""
+    from diver_gb300 import scenes
+    from diver_gb300.realtime import RealtimeModel, convert
+
+    sc = scenes.grid_scene(256, 32, "diver32", device="cuda")
+    sd = {"voxels": sc.features}
+    sd.update(sc.decoder.state_dict())
+    model = RealtimeModel.from_serialized(convert(sd, sc.mask.float()), 256, sc.xyzmin, sc.voxel_size, "cuda")
+    c2w = scenes.sphere_cameras(100, 4.0, 3)[5]
+    _, v = scenes.camera_rays(c2w, 800, 800, 960.0, "cuda")
+    ref, r0 = model.render_frame(c2w[:, 3], v, mode="loop")
+    got, r1 = model.render_frame(c2w[:, 3], v, mode="tc")
+    err = (got - ref).abs().max(1).values.cpu().numpy()
+    print(f"RTTC256 max_abs={err.max():.2e} over_tol={float((err > MLP_EVAL_TOL).mean()):.2e} rounds={r0},{r1}")
+    assert (err > MLP_EVAL_TOL).mean() <= MLP_EVAL_FLIPS
+    assert int(model.tc_err.item()) == 0

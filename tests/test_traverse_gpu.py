@@ -195,8 +195,8 @@ def test_full_frame_walks_stay_within_their_step_bound():
     sd = {"voxels": sc.features}
     sd.update(sc.decoder.state_dict())
     model = RealtimeModel.from_serialized(convert(sd, sc.mask.float()), 256, sc.xyzmin, sc.voxel_size, "cuda")
-    model.render_frame(c2w[:, 3].cuda(), v)
-    model.render_frame(c2w[:, 3].cuda(), v, fused=False)
+    model.render_frame(c2w[:, 3].cuda(), v, mode="fused")
+    model.render_frame(c2w[:, 3].cuda(), v, mode="loop")
     torch.cuda.synchronize()
     assert N.lib().dv_walk_cap_hits(1) == 0
 
