@@ -9,7 +9,7 @@
 //
 // One CTA handles tiles of 128 pixels (thread t = pixel = TMEM lane t); per
 // hit slot k = 0..7 the pixels' k-th hits are the rows of an M = 128 tile:
-//   integral   FP32 on CUDA cores (each thread its own hit's 8 corner rows)
+//   integral   FP32 on CUDA cores, 8 threads per row (coalesced corner rows)
 //   L0         relu(integral) (DIVeR64: the integral itself) x W0^T + bias
 //   L1         relu(h1) x [W2 hidden part | sigma weights]^T: h2 and sigma in
 //              one MMA chain; the PE term of h2 is the pixel's own constant
@@ -145,6 +145,46 @@ __device__ __forceinline__ void put_row3(uint8_t* sA, uint32_t tstride, int t, c
   }
 }
 
+// The tile's integrals, written as the A operand (three terms, K = 32
+// columns): each pixel's hit k (coords and a flag in sHit, 8 floats per row)
+// is integrated by 8 threads, each reading 16 bytes of every corner row, so a
+// warp's loads cover 4 whole rows (coalesced).  FIRST: the integral starts
+// from the pre-multiplied first layer's bias and goes through relu; rows
+// without a hit are zero.
+template <int FIRST>
+__device__ __forceinline__ void integrate_tile(const Args& a, const float* sHit, const float* b_in, uint8_t* sA,
+                                               uint32_t tstride) {
+  const int t = threadIdx.x, q = t & 7;
+#pragma unroll 1
+  for (int p = 0; p < 8; ++p) {
+    const int row = p * 16 + (t >> 3);
+    const float* h = sHit + row * 8;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (h[6] != 0.f) {
+      const SegCorner sc = segment_corners(h[0], h[1], h[2], h[3], h[4], h[5], 1 << 30, 1 << 30, 1 << 30);
+      float4 v[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int x = clampi(sc.x + (j & 1), a.ms - 1);
+        const int yy = clampi(sc.y + ((j >> 1) & 1), a.ms - 1);
+        const int z = clampi(sc.z + (j >> 2), a.ms - 1);
+        const int idx = __ldg(a.vmap + ((long long)z * a.ms + yy) * a.ms + x);
+        v[j] = __ldg(reinterpret_cast<const float4*>(a.feats + (long long)idx * 32) + q);
+      }
+      if (FIRST) f = *reinterpret_cast<const float4*>(b_in + 4 * q);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) fma4(f, sc.w[j], v[j]);
+      if (FIRST) f = make_float4(fmaxf(f.x, 0.f), fmaxf(f.y, 0.f), fmaxf(f.z, 0.f), fmaxf(f.w, 0.f));
+    }
+    uint32_t x[3], y[3];
+    tc::split_pair<3>(f.x, f.y, x);
+    tc::split_pair<3>(f.z, f.w, y);
+    uint8_t* dst = sA + tc::kmajor_offset(row, 4 * q, 32);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) *reinterpret_cast<uint2*>(dst + i * tstride) = make_uint2(x[i], y[i]);
+  }
+}
+
 __device__ __forceinline__ void sync_for_mma() {
   tc::fence_before_sync();
   tc::fence_async_smem();
@@ -157,8 +197,9 @@ struct Bias {
   static constexpr int b_in = 0, l0_b = 32, sig_b = 32 + W, l3_b = 36 + W, size = 40 + W;
 };
 
+// Registers capped for 4 CTAs per SM at width 32 (shared memory allows 5).
 template <int W, int FIRST, int NCOLS>
-__global__ void __launch_bounds__(128) mlp_eval_tc_kernel(const Args a) {
+__global__ void __launch_bounds__(128, W == 32 ? 4 : 1) mlp_eval_tc_kernel(const Args a) {
   using L = RtLayout<W, FIRST>;
   using I = Img<W>;
   using Bi = Bias<W>;
@@ -168,7 +209,8 @@ __global__ void __launch_bounds__(128) mlp_eval_tc_kernel(const Args a) {
   uint8_t* sB = smem;
   uint8_t* sA = smem + 3 * I::TERM;
   float* sb = reinterpret_cast<float*>(sA + 3 * TSTRIDE);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sb + (Bi::size + 3) / 4 * 4);
+  float* sHit = sb + (Bi::size + 3) / 4 * 4;  // [128][8]: this hit's coords and a hit flag per pixel
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sHit + 128 * 8);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   const int t = threadIdx.x, warp = t >> 5;
   for (int i = t; i < 3 * I::TERM / 16; i += 128)
@@ -227,48 +269,20 @@ __global__ void __launch_bounds__(128) mlp_eval_tc_kernel(const Args a) {
 #pragma unroll 1
     for (int k = 0; k < 8; ++k) {
       bool hit = false;
-      float c[6];
       if (alive) {
         const float* cp = a.coords + k * stride + b * 6;
-        c[0] = __ldg(cp);
-        if (c[0] < 0.f) {  // the ray left the grid before its k-th hit
+        if (__ldg(cp) < 0.f) {  // the ray left the grid before its k-th hit
           alive = false;
           fin = true;
         } else {
           hit = true;
 #pragma unroll
-          for (int i = 1; i < 6; ++i) c[i] = __ldg(cp + i);
+          for (int i = 0; i < 6; ++i) sHit[t * 8 + i] = __ldg(cp + i);
         }
       }
+      sHit[t * 8 + 6] = hit ? 1.f : 0.f;
       if (!__syncthreads_or(hit)) break;
-      // integral of the sparse feature table (FP32), texture-style clamped lookups
-      {
-        float f[32];
-#pragma unroll
-        for (int q = 0; q < 32; ++q) f[q] = FIRST ? sb[Bi::b_in + q] : 0.f;
-        if (hit) {
-          const SegCorner sc = segment_corners(c[0], c[1], c[2], c[3], c[4], c[5], 1 << 30, 1 << 30, 1 << 30);
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int x = clampi(sc.x + (j & 1), a.ms - 1);
-            const int yy = clampi(sc.y + ((j >> 1) & 1), a.ms - 1);
-            const int z = clampi(sc.z + (j >> 2), a.ms - 1);
-            const int idx = __ldg(a.vmap + ((long long)z * a.ms + yy) * a.ms + x);
-            const float4* row = reinterpret_cast<const float4*>(a.feats + (long long)idx * 32);
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const float4 w = __ldg(row + q);
-              f[4 * q] = fmaf(sc.w[j], w.x, f[4 * q]);
-              f[4 * q + 1] = fmaf(sc.w[j], w.y, f[4 * q + 1]);
-              f[4 * q + 2] = fmaf(sc.w[j], w.z, f[4 * q + 2]);
-              f[4 * q + 3] = fmaf(sc.w[j], w.w, f[4 * q + 3]);
-            }
-          }
-        }
-#pragma unroll
-        for (int q = 0; q < 32; ++q) f[q] = (FIRST && hit) ? fmaxf(f[q], 0.f) : (hit ? f[q] : 0.f);
-        put_row3<32, 32>(sA, TSTRIDE, t, f);
-      }
+      integrate_tile<FIRST>(a, sHit, sb + Bi::b_in, sA, TSTRIDE);
       sync_for_mma();
       // L0: h1 = W0 x + b0, relu
       ok = __syncthreads_and(tc_layer3<32, W, I::TERM>(sA, TSTRIDE, sB, I::off0, tmem, bar, phase));
@@ -345,7 +359,8 @@ int launch(const Args& a, cudaStream_t st) {
   using I = Img<W>;
   constexpr int NCOLS = W == 32 ? 64 : 128;
   constexpr int KMAX = W > 32 ? W : 32;
-  const size_t smem = 3 * (size_t)I::TERM + 3 * (size_t)128 * KMAX * 2 + (size_t)(Bias<W>::size + 3) / 4 * 16 + 16;
+  const size_t smem = 3 * (size_t)I::TERM + 3 * (size_t)128 * KMAX * 2 + (size_t)(Bias<W>::size + 3) / 4 * 16 +
+                      128 * 8 * 4 + 16;
   auto k = mlp_eval_tc_kernel<W, FIRST, NCOLS>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return DV_ERR_CUDA;
