@@ -19,6 +19,7 @@
 #include "mlp.cuh"
 #include "tc.cuh"
 
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -508,6 +509,33 @@ static int decode_fwd_tc_args(TcArgs& a, int kind, int channels, int terms, cons
   return DV_OK;
 }
 
+// Weight image gather for a refresh after an optimizer step: out term t, entry
+// i = term t of ext[index[i]], where ext[0] = 0 and ext[j] = params[j - 1].
+// form 0: FP32 (biases), 1: BF16, 2: FP16, 3: three BF16 terms, each the
+// round-to-nearest-even of what the previous ones left (the residuals are
+// exact in FP32), term t at out + t * n * 2 bytes.
+__global__ void tc_image_kernel(const float* __restrict__ params, long long n_params,
+                                const int64_t* __restrict__ index, long long n, int form, void* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long j = index[i];
+    const float x = (j > 0 && j <= n_params) ? params[j - 1] : 0.f;
+    if (form == 0) {
+      static_cast<float*>(out)[i] = x;
+    } else if (form == 2) {
+      static_cast<__half*>(out)[i] = __float2half_rn(x);
+    } else {
+      __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out);
+      float r = x;
+      const int terms = form == 3 ? 3 : 1;
+      for (int t = 0; t < terms; ++t) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(r);
+        o[t * n + i] = b;
+        r = __fsub_rn(r, __bfloat162float(b));
+      }
+    }
+  }
+}
+
 extern "C" {
 
 int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,
@@ -566,6 +594,17 @@ long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg) {
   if (d1 < 0 || n_seg < 0) return -1;
   const long long record = 256LL * (channels + (d1 + 2) * kind);
   return (n_seg + 127) / 128 * record;
+}
+
+int dv_tc_image(const float* params, long long n_params, const int64_t* index, long long n, int form, void* out,
+                void* stream) {
+  DV_CHECK(n >= 0 && n_params >= 0 && form >= 0 && form <= 3, DV_ERR_ARG);
+  if (n == 0) return DV_OK;
+  DV_CHECK(index && out && (params || n_params == 0), DV_ERR_ARG);
+  const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 4LL * 152);
+  tc_image_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(params, n_params, index, n, form, out);
+  DV_TRY_LAUNCH();
+  return DV_OK;
 }
 
 }  // extern "C"

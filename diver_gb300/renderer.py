@@ -67,17 +67,6 @@ def _check_params(kind: int, channels: int, params: torch.Tensor):
 FORMS = ("fp32", "bf16", "fp16", "bf16s")
 
 
-def split_terms(x: torch.Tensor, n: int) -> list[torch.Tensor]:
-    """FP32 values as n BF16 terms (each rounds what the previous ones left;
-    every residual is exact in FP32): their sum is x within 2^-(8n) of |x|."""
-    out, r = [], x.float()
-    for _ in range(n):
-        t = r.to(torch.bfloat16)
-        out.append(t)
-        r = r - t.float()
-    return out
-
-
 class TcWeights:
     """Decoder weights in the tensor-core operand layout on the device.  The
     images are gathered from the packed plain parameters on the device
@@ -116,22 +105,20 @@ class TcWeights:
         tw.refresh(pack_plain(decoder).to(device))
         return tw
 
-    def _fill(self, blob: torch.Tensor, values: torch.Tensor) -> None:
-        if self.terms == 1:
-            blob.view(self.dtype).copy_(values)
-            return
-        n = values.numel()
-        for i, t in enumerate(split_terms(values, self.terms)):
-            blob.view(torch.bfloat16)[i * n:(i + 1) * n].copy_(t)
+    def _fill(self, blob: torch.Tensor, index: torch.Tensor, params: torch.Tensor, form: int) -> None:
+        _timed("dv_tc_image", N.ptr(params), params.numel(), N.ptr(index), index.numel(), form, N.ptr(blob),
+               N.stream(params.device))
 
     def refresh(self, params: torch.Tensor) -> None:
-        """Rebuilds the images from the packed plain parameters (device ops only)."""
-        p = params.detach().reshape(-1)
-        ext = torch.cat([p.new_zeros(1), p])
-        self._fill(self.blob, ext[self._i_fwd])
-        self.bias.copy_(ext[self._i_bias])
+        """Rebuilds the images from the packed plain parameters: one gather
+        launch per image (dv_tc_image), no host round trip."""
+        p = params.detach().reshape(-1).contiguous()
+        N.need_cuda("params", p, torch.float32)
+        form = 3 if self.terms > 1 else (2 if self.mode == "fp16" else 1)
+        self._fill(self.blob, self._i_fwd, p, form)
+        self._fill(self.bias, self._i_bias, p, 0)
         if self.bwd is not None:
-            self._fill(self.bwd[0], ext[self._i_bwd])
+            self._fill(self.bwd[0], self._i_bwd, p, form)
 
     def save_buffer(self, kind: int, channels: int, n_seg: int, device) -> torch.Tensor | None:
         """Buffer for the forward's layer inputs, read back by the tensor-core

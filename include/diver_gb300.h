@@ -338,6 +338,18 @@ DV_API int dv_decode_fwd_tc_split(int kind, int channels, const void* wblob, int
 DV_API long long dv_decode_tc_split_save_bytes(int kind, int channels, long long n_seg);
 
 /*
+ * Weight image gather (no counterpart in the reference, whose decoder reads
+ * the FP32 parameters directly): out[i] = ext[index[i]] with ext[0] = 0 and
+ * ext[j] = params[j - 1], converted by form: 0 FP32, 1 BF16, 2 FP16, 3 three
+ * BF16 terms (term t, the round-to-nearest-even of what terms 0..t-1 left, at
+ * out + t * n * 2 bytes).  One launch rebuilds a tensor-core weight image (or
+ * the bias vector) from the packed plain parameters after an optimizer step;
+ * indices outside 0..n_params read 0.
+ */
+DV_API int dv_tc_image(const float* params, long long n_params, const int64_t* index, long long n,
+                       int form, void* out, void* stream);
+
+/*
  * Allocation-free form of dv_exclusive_scan (no counterpart in the reference,
  * which allocates all its buffers with torch).  For callers that cannot
  * allocate device memory themselves — an embedding host whose allocator owns

@@ -135,3 +135,39 @@ def test_split_render_error_vs_fp64_oracle():
     L = [(w.double(), b.double()) for w, b in sc.decoder.layers]
     ref, _, _ = torch_ref.forward(sc.features.double(), L, 3, segs, ray, torch.from_numpy(num), v.double())
     assert np.abs(rgb.cpu().numpy() - ref.numpy()).max() < 1e-5
+
+
+def split_terms(x: torch.Tensor, n: int) -> list[torch.Tensor]:
+    """FP32 values as n BF16 terms, each rounding what the previous ones left."""
+    out, r = [], x.float()
+    for _ in range(n):
+        t = r.to(torch.bfloat16)
+        out.append(t)
+        r = r - t.float()
+    return out
+
+
+def test_weight_image_gather_matches_torch_conversions():
+    """dv_tc_image (the one-launch weight refresh) against torch's own
+    conversions, bit for bit: FP32, BF16, FP16 and the three-term split, with
+    index 0 the zero entry and indices past the parameters reading 0."""
+    from diver_gb300 import _native as N
+
+    g = torch.Generator().manual_seed(3)
+    params = (torch.randn(5000, generator=g) * torch.exp(torch.randn(5000, generator=g) * 4)).cuda()
+    index = torch.randint(0, 5001, (70001,), generator=g)
+    index[:7] = torch.tensor([0, 1, 5000, 5001, 9999, -3, 0])
+    ext = torch.cat([params.new_zeros(1), params])
+    ref = ext[index.clamp(0, 5000).cuda()]
+    ref[(index > 5000) | (index < 0)] = 0
+    index = index.cuda()
+    n = index.numel()
+    st = N.stream()
+    for form, expect in ((0, [ref]), (1, [ref.to(torch.bfloat16)]), (2, [ref.half()]), (3, split_terms(ref, 3))):
+        out = torch.full((len(expect) * n,), -1.0, dtype=expect[0].dtype, device="cuda")
+        N.call("dv_tc_image", N.ptr(params), params.numel(), N.ptr(index), n, form, N.ptr(out), st)
+        torch.cuda.synchronize()
+        assert torch.equal(out.view(torch.int16 if out.element_size() == 2 else torch.int32),
+                           torch.cat(expect).view(torch.int16 if out.element_size() == 2 else torch.int32)), form
+    with pytest.raises(RuntimeError):
+        N.call("dv_tc_image", N.ptr(params), params.numel(), N.ptr(index), n, 4, N.ptr(out), st)
