@@ -55,9 +55,19 @@ struct TcArgs {
   int save_bytes;      // bytes per tile record (sum of 256 * K over the layers)
 };
 
+// Address of term i of element (r, c) of an A tile with K columns.  One term:
+// a [128][K] K-major tile at sA.  Three terms: terms 0 and 1 side by side in
+// one [128][2K] tile at sA (columns i * K + c; the two-term copy of the layer
+// input that the training backward reads back, saved with one bulk copy),
+// term 2 in a [128][K] tile of its own at sA + 2 * tstride.
+template <int TERMS>
+__device__ __forceinline__ uint8_t* a_term(uint8_t* sA, uint32_t tstride, int r, int c, int K, int i) {
+  if constexpr (TERMS == 1) return sA + tc::kmajor_offset(r, c, K);
+  return i < 2 ? sA + tc::kmajor_offset(r, i * K + c, 2 * K) : sA + 2 * tstride + tc::kmajor_offset(r, c, K);
+}
+
 // Gather from the FP32 grid: C/4 threads per segment, each integrating 4
-// channels; the feature row goes to the A tile as TERMS operand terms (tile
-// term i at sA + i * tstride).
+// channels; the feature row goes to the A tile as TERMS operand terms (a_term).
 template <int C, int BF16, int TERMS>
 __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, long long s0, uint8_t* sA,
                                                uint32_t tstride) {
@@ -76,15 +86,16 @@ __device__ __forceinline__ void gather_tile_lp(const TcArgs& a, long long S, lon
                                            __ldg(sg + 5), a.nvx, a.nvy, a.nvz);
       f = integrate4(a.grid, sc, C, q, a.nvx, a.nvy);
     }
-    uint8_t* dst = sA + tc::kmajor_offset(ls, 4 * q, C);
     if constexpr (TERMS == 1) {
-      *reinterpret_cast<uint2*>(dst) = make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
+      *reinterpret_cast<uint2*>(a_term<1>(sA, tstride, ls, 4 * q, C, 0)) =
+          make_uint2(tc::pack2<BF16>(f.x, f.y), tc::pack2<BF16>(f.z, f.w));
     } else {
       uint32_t x[TERMS], y[TERMS];
       tc::split_pair<TERMS>(f.x, f.y, x);
       tc::split_pair<TERMS>(f.z, f.w, y);
 #pragma unroll
-      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint2*>(dst + i * tstride) = make_uint2(x[i], y[i]);
+      for (int i = 0; i < TERMS; ++i)
+        *reinterpret_cast<uint2*>(a_term<TERMS>(sA, tstride, ls, 4 * q, C, i)) = make_uint2(x[i], y[i]);
     }
   }
 }
@@ -129,9 +140,10 @@ __device__ __forceinline__ void gather_tile_lp_x2(const TcArgs& a, long long S, 
       uint32_t x[TERMS], y[TERMS];
       tc::split_pair<TERMS>(f.x, f.y, x);
       tc::split_pair<TERMS>(f.z, f.w, y);
-      uint8_t* dst = sA + tc::kmajor_offset((p + u) * SPP + t / TPS, 4 * q, C);
 #pragma unroll
-      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint2*>(dst + i * tstride) = make_uint2(x[i], y[i]);
+      for (int i = 0; i < TERMS; ++i)
+        *reinterpret_cast<uint2*>(a_term<TERMS>(sA, tstride, (p + u) * SPP + t / TPS, 4 * q, C, i)) =
+            make_uint2(x[i], y[i]);
     }
   }
 }
@@ -193,10 +205,10 @@ __device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long S, lon
 // With TERMS = 3 the A tile and the weight images are three BF16 terms each
 // and the chain sums the six products whose term indices add up to at most 2
 // (FP32-grade products).  With `save`, thread 0 also copies the layer's input
-// tile (the A operand, 256 * K bytes; with TERMS = 3 its first two terms, a
-// two-term split of the same values) to global memory by bulk async copies
-// and, before the caller's barrier lets anyone overwrite A, waits until those
-// copies have read it.
+// tile (the A operand, 256 * K bytes; with TERMS = 3 the [128][2K] tile of its
+// first two terms, a two-term split of the same values) to global memory by a
+// bulk async copy and, before the caller's barrier lets anyone overwrite A,
+// waits until that copy has read it.
 template <int BF16, int TERMS>
 __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, uint32_t wterm, const uint8_t* sA,
                                          uint32_t tstride, uint32_t tmem, uint64_t* bar, uint32_t& phase,
@@ -207,18 +219,20 @@ __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, ui
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
     if (save != nullptr) {
-      tc::bulk_store(save, sA, (uint32_t)L.K * 256u);
-      if (TERMS > 1) tc::bulk_store(save + L.K * 256, sA + tstride, (uint32_t)L.K * 256u);
+      tc::bulk_store(save, sA, (uint32_t)L.K * 256u * (TERMS > 1 ? 2u : 1u));
       tc::bulk_commit();
     }
     const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
     const uint32_t sbo = (uint32_t)(L.K / 8) * 128;
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
-      const uint32_t a0 = tc::smem_u32(sA + PA[p] * tstride), b0 = tc::smem_u32(sB + PB[p] * wterm + L.b_off);
+      // A term PA[p] (a_term's layout): terms 0 and 1 are K-column slices of the [128][2K] tile
+      const bool wide = TERMS > 1 && PA[p] < 2;
+      const uint32_t a0 = tc::smem_u32(wide ? sA + PA[p] * (L.K / 8) * 128 : sA + (TERMS > 1 ? 2 * tstride : 0));
+      const uint32_t b0 = tc::smem_u32(sB + PB[p] * wterm + L.b_off);
       for (int k = 0; k < L.K / 16; ++k)
-        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
-                    (p > 0 || k > 0) ? 1u : 0u);
+        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, wide ? 2 * sbo : sbo), tc::smem_desc(b0 + k * 256, 128, sbo),
+                    idesc, (p > 0 || k > 0) ? 1u : 0u);
     }
     tc::mma_commit(bar);
   }
@@ -230,19 +244,18 @@ __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, ui
 }
 
 // Writes 32 values (columns c0..c0+31 of the next layer's input) of row t,
-// as TERMS operand terms (term i at sA + i * tstride).
+// as TERMS operand terms (a_term's layout).
 template <int BF16, int TERMS>
 __device__ __forceinline__ void store_row32(uint8_t* sA, uint32_t tstride, int t, int c0, int K, const float* v) {
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    uint8_t* dst = sA + tc::kmajor_offset(t, c0 + 8 * j, K);
     if constexpr (TERMS == 1) {
       uint4 w;
       w.x = tc::pack2<BF16>(v[8 * j + 0], v[8 * j + 1]);
       w.y = tc::pack2<BF16>(v[8 * j + 2], v[8 * j + 3]);
       w.z = tc::pack2<BF16>(v[8 * j + 4], v[8 * j + 5]);
       w.w = tc::pack2<BF16>(v[8 * j + 6], v[8 * j + 7]);
-      *reinterpret_cast<uint4*>(dst) = w;
+      *reinterpret_cast<uint4*>(a_term<1>(sA, tstride, t, c0 + 8 * j, K, 0)) = w;
     } else {
       uint32_t x[TERMS], y[TERMS], z[TERMS], u[TERMS];
       tc::split_pair<TERMS>(v[8 * j + 0], v[8 * j + 1], x);
@@ -250,7 +263,8 @@ __device__ __forceinline__ void store_row32(uint8_t* sA, uint32_t tstride, int t
       tc::split_pair<TERMS>(v[8 * j + 4], v[8 * j + 5], z);
       tc::split_pair<TERMS>(v[8 * j + 6], v[8 * j + 7], u);
 #pragma unroll
-      for (int i = 0; i < TERMS; ++i) *reinterpret_cast<uint4*>(dst + i * tstride) = make_uint4(x[i], y[i], z[i], u[i]);
+      for (int i = 0; i < TERMS; ++i)
+        *reinterpret_cast<uint4*>(a_term<TERMS>(sA, tstride, t, c0 + 8 * j, K, i)) = make_uint4(x[i], y[i], z[i], u[i]);
     }
   }
 }
