@@ -175,36 +175,38 @@ __device__ __forceinline__ void relu_mask(const uint8_t* tile, int r, int c0, fl
 // columns of K, delta_0 x [W0|W1] and delta_1 x [W0|W1] into columns 0..63,
 // delta_0 x W2 into 32..63 and delta_2 x W0 into 0..31.
 __device__ __forceinline__ void mma_prop(uint32_t tmem, const uint8_t* D, const uint8_t* img, int K) {
-  constexpr uint32_t sboA = (DW / 8) * 128;
-  const uint32_t sboB = (uint32_t)(K / 8) * 128;
-  const uint32_t d0 = tc::smem_u32(D), b0 = tc::smem_u32(img), b2 = b0 + 2 * 32 * K * 2;
+  constexpr uint32_t sboA = (DW / 8) * 128, term = (FD / 8) * 128;
+  const uint64_t a0 = tc::smem_desc(tc::smem_u32(D), 128, sboA);
+  const uint64_t b0 = tc::smem_desc(tc::smem_u32(img), 128, (uint32_t)(K / 8) * 128);
   const uint32_t i64 = tc::idesc_f16(128, 64, 1), i32 = tc::idesc_f16(128, 32, 1);
+#pragma unroll
   for (int k = 0; k < K / 16; ++k) {
-    const uint32_t ak = d0 + k * 256, bk = k * 256;
-    tc::mma_f16(tmem, tc::smem_desc(ak, 128, sboA), tc::smem_desc(b0 + bk, 128, sboB), i64, k > 0 ? 1u : 0u);
-    tc::mma_f16(tmem, tc::smem_desc(ak + (FD / 8) * 128, 128, sboA), tc::smem_desc(b0 + bk, 128, sboB), i64, 1u);
-    tc::mma_f16(tmem + 32, tc::smem_desc(ak, 128, sboA), tc::smem_desc(b2 + bk, 128, sboB), i32, 1u);
-    tc::mma_f16(tmem, tc::smem_desc(ak + 2 * (FD / 8) * 128, 128, sboA), tc::smem_desc(b0 + bk, 128, sboB), i32, 1u);
+    const uint64_t ak = tc::desc_plus(a0, k * 256), bk = tc::desc_plus(b0, k * 256);
+    tc::mma_f16(tmem, ak, bk, i64, k > 0 ? 1u : 0u);
+    tc::mma_f16(tmem, tc::desc_plus(ak, term), bk, i64, 1u);
+    tc::mma_f16(tmem + 32, ak, tc::desc_plus(bk, 2 * 32 * K * 2), i32, 1u);
+    tc::mma_f16(tmem, tc::desc_plus(ak, 2 * term), bk, i32, 1u);
   }
 }
 
 // Transposed view of the delta tile as the A operand of the gradient MMAs:
 // M = 128 rows = delta tile columns 0..127 (terms 0 and 1 in rows 0..47 and
 // 48..95), K = 16 segments per MMA.
-__device__ __forceinline__ uint64_t delta_t_desc(const uint8_t* D, int k) {
+__device__ __forceinline__ uint64_t delta_t_desc(const uint8_t* D) {
   constexpr uint32_t lbo = (DW / 8) * 128;  // next 8 segments
-  return tc::smem_desc(tc::smem_u32(D) + k * 2 * lbo, lbo, 128);
+  return tc::smem_desc(tc::smem_u32(D), lbo, 128);
 }
+constexpr uint32_t DELTA_T_K = 2 * (DW / 8) * 128;  // bytes per 16 segments of that view
 
 // Weight gradient over the tile's 128 segments: TMEM dW[128][64] +=
 // delta^T x act, act a [128][2 x 32] tile read transposed (N = 64: both terms).
 __device__ __forceinline__ void mma_dw(uint32_t tmem, const uint8_t* D, const uint8_t* act, bool accumulate) {
   const uint32_t idesc = tc::idesc_f16(128, 64, 1) | (1u << 15) | (1u << 16);
   constexpr uint32_t lboB = (64 / 8) * 128;
-  const uint32_t b0 = tc::smem_u32(act);
+  const uint64_t a0 = delta_t_desc(D), b0 = tc::smem_desc(tc::smem_u32(act), lboB, 128);
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    tc::mma_f16(tmem, delta_t_desc(D, k), tc::smem_desc(b0 + k * 2 * lboB, lboB, 128), idesc,
+    tc::mma_f16(tmem, tc::desc_plus(a0, k * DELTA_T_K), tc::desc_plus(b0, k * 2 * lboB), idesc,
                 (accumulate || k > 0) ? 1u : 0u);
 }
 
@@ -215,10 +217,10 @@ __device__ __forceinline__ void mma_dw(uint32_t tmem, const uint8_t* D, const ui
 __device__ __forceinline__ void mma_db(uint32_t tmem, const uint8_t* D, const uint8_t* ones, bool accumulate) {
   const uint32_t idesc = tc::idesc_f16(128, 16, 1) | (1u << 15) | (1u << 16);
   constexpr uint32_t lboB = (16 / 8) * 128;
-  const uint32_t b0 = tc::smem_u32(ones);
+  const uint64_t a0 = delta_t_desc(D), b0 = tc::smem_desc(tc::smem_u32(ones), lboB, 128);
 #pragma unroll
   for (int k = 0; k < 8; ++k)
-    tc::mma_f16(tmem, delta_t_desc(D, k), tc::smem_desc(b0 + k * 2 * lboB, lboB, 128), idesc,
+    tc::mma_f16(tmem, tc::desc_plus(a0, k * DELTA_T_K), tc::desc_plus(b0, k * 2 * lboB), idesc,
                 (accumulate || k > 0) ? 1u : 0u);
 }
 

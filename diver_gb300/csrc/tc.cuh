@@ -34,6 +34,11 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
   return d;  // base offset 0, LBO mode 0, no swizzle
 }
 
+// The descriptor of an operand `bytes` further on (a multiple of 16): the
+// start address is the low field (address / 16, 14 bits), and shared-memory
+// addresses stay below 256 KiB, so the add never carries out of it.
+__device__ __forceinline__ uint64_t desc_plus(uint64_t d, uint32_t bytes) { return d + (bytes >> 4); }
+
 // Instruction descriptor for kind::f16: D FP32, A/B both BF16 (bf16 = 1) or
 // both FP16 (bf16 = 0), both K-major, shape M x N.
 __host__ __device__ __forceinline__ uint32_t idesc_f16(int M, int N, int bf16) {

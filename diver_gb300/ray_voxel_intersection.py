@@ -178,30 +178,60 @@ def _buffers(S: int, dev):
             torch.empty(S, dtype=torch.int32, device=dev))
 
 
+class SlotWalk:
+    """The first half of a fixed-capacity masked traversal: every ray's
+    segments in its own range of `slot` rows, the per-ray counts, their
+    exclusive scan and the longest ray, all on the device."""
+
+    __slots__ = ("sseg", "st", "num", "offsets", "mx", "slot", "S")
+
+    def __init__(self, sseg, st, num, offsets, mx, slot, S):
+        self.sseg, self.st, self.num, self.offsets, self.mx, self.slot, self.S = sseg, st, num, offsets, mx, slot, S
+
+
+def masked_slot_walk(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity: int) -> SlotWalk:
+    """Walks the rays into per-ray slots (dv_masked_segments_slots) and scans
+    the counts on the device; compact_slot_walk turns the result into CSR
+    segments."""
+    B = _check_rays(o, v)
+    m8 = _check_mask(mask, voxel_num, mask_scale)
+    dev = o.device
+    S = _capacity(capacity, B, 3 * int(voxel_num))
+    slot = 3 * int(voxel_num) + 3
+    num = torch.empty(B, dtype=torch.int32, device=dev)
+    mx = torch.zeros(1, dtype=torch.int32, device=dev)
+    sseg = torch.empty(B * slot, 6, dtype=torch.float32, device=dev)
+    st = torch.empty(B * slot, dtype=torch.float32, device=dev)
+    if B > 0:
+        N.call("dv_masked_segments_slots", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+               N.ptr(o), N.ptr(v), N.ptr(m8), slot, N.ptr(sseg), N.ptr(st), N.ptr(num), N.ptr(mx), N.stream(dev))
+    return SlotWalk(sseg, st, num, exclusive_scan(num), mx, slot, S)
+
+
+def compact_slot_walk(w: SlotWalk) -> Segments:
+    """CSR segments of a slot walk (dv_compact_slots), in buffers of the walk's capacity."""
+    B = w.num.numel()
+    dev = w.num.device
+    seg, t, ray = _buffers(w.S, dev)
+    if B > 0:
+        N.call("dv_compact_slots", B, w.slot, N.ptr(w.offsets), N.ptr(w.sseg), N.ptr(w.st), N.ptr(seg), N.ptr(t),
+               N.ptr(ray), N.stream(dev))
+    return Segments(w.offsets, seg, t, ray, w.num, None, w.mx)
+
+
 def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity: int | None = None) -> Segments:
     """Segments of occupied voxels; equals coord[mask] of masked_intersect's output
     (model/diver.py:86-93), t = exit distance.  With `capacity`: fixed-size
     buffers, no host read (see Segments)."""
+    if capacity is not None and o.shape[0] > 0:
+        # fixed capacity: one walk writes every ray into its own range of rows
+        # (slots), then the slots are compacted into the CSR lists
+        return compact_slot_walk(masked_slot_walk(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity))
     B = _check_rays(o, v)
     m8 = _check_mask(mask, voxel_num, mask_scale)
     dev = o.device
     st = N.stream(dev)
     num = torch.empty(B, dtype=torch.int32, device=dev)
-    if capacity is not None and B > 0:
-        # fixed capacity: one walk writes every ray into its own range of rows
-        # (slots), then the slots are compacted into the CSR lists
-        S = _capacity(capacity, B, 3 * int(voxel_num))
-        slot = 3 * int(voxel_num) + 3
-        mx = torch.zeros(1, dtype=torch.int32, device=dev)
-        sseg = torch.empty(B * slot, 6, dtype=torch.float32, device=dev)
-        st_ = torch.empty(B * slot, dtype=torch.float32, device=dev)
-        N.call("dv_masked_segments_slots", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-               N.ptr(o), N.ptr(v), N.ptr(m8), slot, N.ptr(sseg), N.ptr(st_), N.ptr(num), N.ptr(mx), st)
-        offsets = exclusive_scan(num)
-        seg, t, ray = _buffers(S, dev)
-        N.call("dv_compact_slots", B, slot, N.ptr(offsets), N.ptr(sseg), N.ptr(st_), N.ptr(seg), N.ptr(t), N.ptr(ray),
-               st)
-        return Segments(offsets, seg, t, ray, num, None, mx)
     last = torch.empty(B, dtype=torch.int32, device=dev)  # where each ray's emission walk may stop
     mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
     N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),

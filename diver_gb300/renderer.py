@@ -367,13 +367,15 @@ class DIVeRField(torch.nn.Module):
                N.ptr(alpha_map), st)
 
     def forward(self, os: torch.Tensor, ds: torch.Tensor, form: str = "fp32", capacity: int | None = None,
-                grad_voxels=None):
+                grad_voxels=None, segments: Segments | None = None):
         """(rgb [B,3], sparsity term); reference DIVeR.forward + render (model/diver.py:141-207).
         form: 'fp32' (plain), 'bf16' or 'fp16' (tensor-core decoder; without
         autograd they read a 16-bit copy of the grid) or 'bf16s' (tensor-core
         decoder with split BF16 operands: FP32-grade, the accurate training form).
         capacity: fixed segment buffers, no host synchronisation (see segments).
-        grad_voxels: see render_segments."""
+        grad_voxels: see render_segments.
+        segments: the rays' segments when the caller traversed them already
+        (the traversal is then skipped)."""
         os, ds = os.contiguous(), ds.contiguous()
         N.need_cuda("dirs", ds, torch.float32)
         dev = self.voxels.device
@@ -392,7 +394,7 @@ class DIVeRField(torch.nn.Module):
                 _check_params(kind, self.voxels.shape[-1], self.params)
                 _timed("dv_ray_pe", kind, self.voxels.shape[-1], N.ptr(self.params), ds.shape[0], N.ptr(ds),
                        N.ptr(pe[0]), N.ptr(pe[1]), N.stream(dev))
-        seg = self.segments(os, ds, capacity)
+        seg = segments if segments is not None else self.segments(os, ds, capacity)
         main.wait_stream(side)
         g16 = self.grid16(form) if not torch.is_grad_enabled() else None
         return render_segments(self.voxels, self.params, seg, ds, self.kind, self.white_back, tc, g16, grad_voxels,
