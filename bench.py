@@ -79,16 +79,17 @@ def alg_work(kernel, S, U, R):
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per segment of the
 # decode kernels in the captured 4096-ray training step, from ncu captures of
 # `python bench.py --profile train --form <form>`: the single-term BF16 kernels
-# on the 256^3 grid, the split-operand kernels on the 128^3 grid of the same
-# scene family (557,787 segments; their traffic is per-segment: the saved
-# record, the rays' segments and the gradient rows they touch); the roofline's
-# `traffic` is this times the segments of a launch.
-TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52,
-                   "dv_decode_bwd_tc_split": 1405.0, "dv_decode_fwd_tc_split": 990.5}
-# Kernels of this library per captured training step: row clear, ray PE, slot
-# walk, 3 scan kernels, slot compaction, decoder forward, compositing forward,
-# compositing backward, row marking, decoder backward.
-OUR_LAUNCHES_PER_STEP = 12
+# on the 256^3 grid, the split-operand forward on the 128^3 grid of the same
+# scene family (557,787 segments; its traffic is per-segment: the rays'
+# segments, the corner rows and the saved record); the roofline's `traffic`
+# is this times the segments of a launch.  The split backward has no entry:
+# its current form has no ncu section capture (the roofline reports null).
+TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52, "dv_decode_fwd_tc_split": 992.6}
+# Kernels of this library per captured training step: row clear, three weight
+# image gathers, ray PE, slot walk, 3 scan kernels, slot compaction, decoder
+# forward, compositing forward, compositing backward, row marking, decoder
+# backward.
+OUR_LAUNCHES_PER_STEP = 15
 
 
 def parse():

@@ -455,6 +455,33 @@ __global__ void wait_selftest_kernel(uint32_t limit, int* status) {
   status[1] = tc::mbar_wait_bounded(&bar[1], 0, limit) ? 0 : 1;
 }
 
+// Weight image gather for a refresh after an optimizer step: out term t, entry
+// i = term t of ext[index[i]], where ext[0] = 0 and ext[j] = params[j - 1].
+// form 0: FP32 (biases), 1: BF16, 2: FP16, 3: three BF16 terms, each the
+// round-to-nearest-even of what the previous ones left (the residuals are
+// exact in FP32), term t at out + t * n * 2 bytes.
+__global__ void tc_image_kernel(const float* __restrict__ params, long long n_params,
+                                const int64_t* __restrict__ index, long long n, int form, void* out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long j = index[i];
+    const float x = (j > 0 && j <= n_params) ? params[j - 1] : 0.f;
+    if (form == 0) {
+      static_cast<float*>(out)[i] = x;
+    } else if (form == 2) {
+      static_cast<__half*>(out)[i] = __float2half_rn(x);
+    } else {
+      __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out);
+      float r = x;
+      const int terms = form == 3 ? 3 : 1;
+      for (int t = 0; t < terms; ++t) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(r);
+        o[t * n + i] = b;
+        r = __fsub_rn(r, __bfloat162float(b));
+      }
+    }
+  }
+}
+
 }  // namespace dv
 
 using namespace dv;
@@ -523,32 +550,6 @@ static int decode_fwd_tc_args(TcArgs& a, int kind, int channels, int terms, cons
   return DV_OK;
 }
 
-// Weight image gather for a refresh after an optimizer step: out term t, entry
-// i = term t of ext[index[i]], where ext[0] = 0 and ext[j] = params[j - 1].
-// form 0: FP32 (biases), 1: BF16, 2: FP16, 3: three BF16 terms, each the
-// round-to-nearest-even of what the previous ones left (the residuals are
-// exact in FP32), term t at out + t * n * 2 bytes.
-__global__ void tc_image_kernel(const float* __restrict__ params, long long n_params,
-                                const int64_t* __restrict__ index, long long n, int form, void* out) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const long long j = index[i];
-    const float x = (j > 0 && j <= n_params) ? params[j - 1] : 0.f;
-    if (form == 0) {
-      static_cast<float*>(out)[i] = x;
-    } else if (form == 2) {
-      static_cast<__half*>(out)[i] = __float2half_rn(x);
-    } else {
-      __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out);
-      float r = x;
-      const int terms = form == 3 ? 3 : 1;
-      for (int t = 0; t < terms; ++t) {
-        const __nv_bfloat16 b = __float2bfloat16_rn(r);
-        o[t * n + i] = b;
-        r = __fsub_rn(r, __bfloat162float(b));
-      }
-    }
-  }
-}
 
 extern "C" {
 

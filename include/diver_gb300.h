@@ -324,7 +324,9 @@ DV_API long long dv_decode_tc_save_bytes(int kind, int channels, long long n_seg
  * after the other, wbytes apart (wbytes = one term's bytes); `layers`, bias and
  * the rest as dv_decode_fwd_tc; the corner rows come from the FP32 grid.  save
  * (optional, >= dv_decode_tc_split_save_bytes): receives every layer input as
- * two BF16 terms for dv_decode_bwd_tc_split.
+ * two BF16 terms for dv_decode_bwd_tc_split: per tile of 128 segments and
+ * layer, one [128][2K] K-major core-matrix tile (256 * 2K bytes) with term j
+ * in columns jK..jK+K-1.
  */
 DV_API int dv_decode_fwd_tc_split(int kind, int channels, const void* wblob, int wbytes,
                                   const float* bias, int nbias, const int* layers, int n_layers,
@@ -393,8 +395,8 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
  * Deltas propagate through three BF16 terms of each transposed weight image
  * (wb: three terms of dv_decode_bwd_tc's images, wb_term_bytes apart;
  * b_layers: HOST rows of (byte offset inside a term, K, N)) with six products
- * per layer; weight gradients accumulate in FP32 from two-term deltas and
- * activations (three products).  saved: the record dv_decode_fwd_tc_split
+ * per layer; weight and bias gradients accumulate in FP32 from two-term deltas
+ * and activations (all four products).  saved: the record dv_decode_fwd_tc_split
  * wrote for the same segments and weights (saved_bytes >=
  * dv_decode_tc_split_save_bytes), out4 its output; the forward is read back,
  * never recomputed.  Adds into grad_voxels and grad_params like dv_decode_bwd.
