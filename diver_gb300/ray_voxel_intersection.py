@@ -219,33 +219,59 @@ def compact_slot_walk(w: SlotWalk) -> Segments:
     return Segments(w.offsets, seg, t, ray, w.num, None, w.mx)
 
 
+class PendingSegments:
+    """An exact masked traversal whose count walk and scan are queued on the
+    device: finish() reads the total back (one host read) and queues the
+    emission walk.  Launching the count walks of several batches (on their
+    own streams) before finishing any lets them run together."""
+
+    __slots__ = ("args", "num", "offsets", "last")
+
+    def __init__(self, args, num, offsets, last):
+        self.args, self.num, self.offsets, self.last = args, num, offsets, last
+
+    def finish(self) -> Segments:
+        o, v, xyzmin, voxel_num, voxel_size, m8, mask_scale = self.args
+        dev = o.device
+        S, M = _totals(self.offsets, self.num)
+        seg, t, ray = _buffers(S, dev)
+        if S > 0:
+            N.call("dv_masked_segments", self.num.numel(), float(xyzmin), float(voxel_num), float(voxel_size),
+                   float(mask_scale), N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(self.offsets), N.ptr(seg), N.ptr(t),
+                   N.ptr(ray), N.ptr(self.last), N.stream(dev))
+        return Segments(self.offsets, seg, t, ray, self.num, M, None)
+
+
+def masked_segments_begin(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale) -> PendingSegments:
+    """The first half of masked_segments without capacity: count walk and scan."""
+    B = _check_rays(o, v)
+    m8 = _check_mask(mask, voxel_num, mask_scale)
+    dev = o.device
+    num = torch.empty(B, dtype=torch.int32, device=dev)
+    last = torch.empty(B, dtype=torch.int32, device=dev)  # where each ray's emission walk may stop
+    if B > 0:
+        N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
+               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), None, N.ptr(last), N.stream(dev))
+    return PendingSegments((o, v, xyzmin, voxel_num, voxel_size, m8, mask_scale), num, exclusive_scan(num), last)
+
+
 def masked_segments(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity: int | None = None) -> Segments:
     """Segments of occupied voxels; equals coord[mask] of masked_intersect's output
     (model/diver.py:86-93), t = exit distance.  With `capacity`: fixed-size
     buffers, no host read (see Segments)."""
-    if capacity is not None and o.shape[0] > 0:
+    if capacity is None:
+        return masked_segments_begin(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale).finish()
+    if o.shape[0] > 0:
         # fixed capacity: one walk writes every ray into its own range of rows
         # (slots), then the slots are compacted into the CSR lists
         return compact_slot_walk(masked_slot_walk(o, v, xyzmin, voxel_num, voxel_size, mask, mask_scale, capacity))
     B = _check_rays(o, v)
-    m8 = _check_mask(mask, voxel_num, mask_scale)
+    _check_mask(mask, voxel_num, mask_scale)
     dev = o.device
-    st = N.stream(dev)
-    num = torch.empty(B, dtype=torch.int32, device=dev)
-    last = torch.empty(B, dtype=torch.int32, device=dev)  # where each ray's emission walk may stop
-    mx = torch.zeros(1, dtype=torch.int32, device=dev) if capacity is not None else None
-    N.call("dv_masked_count", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-           N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(num), N.ptr(mx), N.ptr(last), st)
-    offsets = exclusive_scan(num)
-    if capacity is None:
-        S, M = _totals(offsets, num)
-    else:
-        S, M = _capacity(capacity, B, 3 * int(voxel_num)), None
+    S = _capacity(capacity, B, 3 * int(voxel_num))
     seg, t, ray = _buffers(S, dev)
-    if S > 0 and B > 0:
-        N.call("dv_masked_segments", B, float(xyzmin), float(voxel_num), float(voxel_size), float(mask_scale),
-               N.ptr(o), N.ptr(v), N.ptr(m8), N.ptr(offsets), N.ptr(seg), N.ptr(t), N.ptr(ray), N.ptr(last), st)
-    return Segments(offsets, seg, t, ray, num, M, mx)
+    return Segments(torch.zeros(1, dtype=torch.int64, device=dev), seg, t, ray,
+                    torch.empty(0, dtype=torch.int32, device=dev), None, torch.zeros(1, dtype=torch.int32, device=dev))
 
 
 def dense_segments(o, v, xyzmin, voxel_num, voxel_size, capacity: int | None = None) -> Segments:

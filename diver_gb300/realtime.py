@@ -148,10 +148,30 @@ class RealtimeModel:
         aabb_intersect(coords, v, center, finish, rgba, self.octrees, self.voxel_num)
         rounds = 0
         limit = max_rounds if max_rounds is not None else 3 * self.voxel_num
-        while rounds < limit and not bool(finish.all()):
+        if mode == "loop":
+            while rounds < limit and not bool(finish.all()):
+                ray_march(coords, v, self.voxel_masks, finish, self.voxel_num)
+                self.mlp_eval(rgba, coords, v, finish, False)
+                rounds += 1
+            return rgba[:, :3] + rgba[:, 3:], rounds
+        # "tc": the host learns one round late that every pixel has finished, so
+        # round k + 1 is queued while it waits for round k's flag (a round after
+        # the last pixel finished changes nothing; the frame is the same, the
+        # round count at most one higher)
+        if getattr(self, "_flags", None) is None:
+            self._flags = (torch.zeros(2, dtype=torch.bool, pin_memory=True), [torch.cuda.Event(), torch.cuda.Event()])
+        flags, events = self._flags
+        while rounds < limit:
             ray_march(coords, v, self.voxel_masks, finish, self.voxel_num)
-            self.mlp_eval(rgba, coords, v, finish, mode == "tc")
+            self.mlp_eval(rgba, coords, v, finish, True)
             rounds += 1
+            slot = rounds % 2
+            flags[slot:slot + 1].copy_(finish.all().reshape(1), non_blocking=True)
+            events[slot].record()
+            if rounds >= 2:
+                events[1 - slot].synchronize()
+                if bool(flags[1 - slot]):
+                    break
         return rgba[:, :3] + rgba[:, 3:], rounds
 
 

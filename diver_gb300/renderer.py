@@ -21,7 +21,8 @@ from torch.autograd import Function
 
 from . import _native as N
 from .decoder import Decoder, pack_plain, tc_index_maps
-from .ray_voxel_intersection import Segments, dense_segments, masked_segments, masked_segments_grid
+from .ray_voxel_intersection import (Segments, dense_segments, masked_segments, masked_segments_begin,
+                                     masked_segments_grid)
 
 KIND_ID = {"diver32": 32, "diver64": 64}
 WIDTH = {32: 32, 64: 64}
@@ -324,6 +325,16 @@ class DIVeRField(torch.nn.Module):
             return masked_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, self.voxel_mask,
                                    self.mask_scale, capacity)
         return dense_segments(os, ds, self.xyzmin, self.voxel_num, self.voxel_size, capacity)
+
+    def begin_segments(self, os: torch.Tensor, ds: torch.Tensor):
+        """Exact segments in two halves: the count walk and scan are queued now and
+        the returned object's finish() reads the total and queues the emission
+        (an occupancy-masked cubic grid; other grids are traversed at once and
+        returned finished)."""
+        if self.aniso or self.voxel_mask is None:
+            return self.segments(os, ds)
+        return masked_segments_begin(os.contiguous(), ds.contiguous(), self.xyzmin, self.voxel_num, self.voxel_size,
+                                     self.voxel_mask, self.mask_scale)
 
     def grid16(self, form: str) -> torch.Tensor | None:
         """BF16/FP16 copy of the feature grid for tensor-core rendering (made

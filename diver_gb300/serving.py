@@ -213,26 +213,44 @@ class GpuRenderer:
 
     def render(self, field_model, work: list[tuple[Request, int, int]]):
         """Launches one batch for all chunks in `work` on the scene's stream; returns
-        (event, [(request, first, count, rgb view)])."""
-        dev = field_model.voxels.device
-        st = self.stream(work[0][0].scene)
-        with torch.cuda.stream(st):
-            os_, ds_ = zip(*(self.rays_for(r, a, n, dev) for r, a, n in work))
-            o = torch.cat(os_)
-            d = torch.cat(ds_)
-            with torch.no_grad():
-                rgb, _ = field_model(o, d, form=self.form)
-            out = []
-            k = 0
-            for r, a, n in work:
-                if r.rgb is None:
-                    r.rgb = torch.empty(r.rays, 3, device=dev)
-                r.rgb[a:a + n].copy_(rgb[k:k + n])
-                out.append((r, a, n))
-                k += n
-            ev = torch.cuda.Event()
-            ev.record(st)
-        return ev, out
+        (event, [(request, first, count)])."""
+        return self.render_many([(field_model, work)])[0]
+
+    def render_many(self, batches) -> list:
+        """Launches one batch per scene ([(model, work), ...]), each on its scene's
+        stream, in two passes: first every batch's rays and traversal count walk,
+        then, scene by scene, the total's host read, the emission walk, decode and
+        compositing.  The count walks (one warp per SM each) of all scenes run
+        together, and the host reads a total only once its walk has had the time
+        of the others' launches.  Returns [(event, [(request, first, count)])]."""
+        began = []
+        for field_model, work in batches:
+            dev = field_model.voxels.device
+            st = self.stream(work[0][0].scene)
+            with torch.cuda.stream(st):
+                os_, ds_ = zip(*(self.rays_for(r, a, n, dev) for r, a, n in work))
+                o = torch.cat(os_)
+                d = torch.cat(ds_)
+                began.append((field_model, work, st, o, d, field_model.begin_segments(o, d)))
+        out = []
+        for field_model, work, st, o, d, pending in began:
+            dev = field_model.voxels.device
+            with torch.cuda.stream(st):
+                seg = pending.finish() if hasattr(pending, "finish") else pending
+                with torch.no_grad():
+                    rgb, _ = field_model(o, d, form=self.form, segments=seg)
+                done = []
+                k = 0
+                for r, a, n in work:
+                    if r.rgb is None:
+                        r.rgb = torch.empty(r.rays, 3, device=dev)
+                    r.rgb[a:a + n].copy_(rgb[k:k + n])
+                    done.append((r, a, n))
+                    k += n
+                ev = torch.cuda.Event()
+                ev.record(st)
+            out.append((ev, done))
+        return out
 
 
 def serve(requests: list[Request], residency: Residency, renderer: GpuRenderer, realtime: bool = True,
@@ -252,9 +270,10 @@ def serve(requests: list[Request], residency: Residency, renderer: GpuRenderer, 
             # with nothing running, admission only fails when the scene cannot fit the budget
             raise RuntimeError("requests cannot be admitted: scene larger than the free HBM budget")
         batches = sch.next_batches()
-        for scene, work in batches.items():
-            model = residency.scenes[scene].resident
-            inflight.append(renderer.render(model, work))
+        if batches:
+            items = [(residency.scenes[scene].resident, work) for scene, work in batches.items()]
+            many = getattr(renderer, "render_many", None)  # one pass over all scenes when the renderer has it
+            inflight.extend(many(items) if many else [renderer.render(m, w) for m, w in items])
         # retire finished batches (poll; block only if nothing else can progress)
         if not batches and inflight:
             inflight[0][0].synchronize()

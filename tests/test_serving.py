@@ -23,6 +23,9 @@ class FakeRenderer:
         self.batches.append([(r.rid, a, n) for r, a, n in work])
         return Done(), work
 
+    def render_many(self, batches):
+        return [self.render(model, work) for model, work in batches]
+
 
 def test_residency_admits_by_budget_and_evicts_idle_lru():
     loads = []
