@@ -32,6 +32,7 @@ struct TcLayer {
   int b_off;     // byte offset of the layer's B image in the weight blob
   int K, N;      // padded: K % 16 == 0, N % 16 == 0
   int bias_off;  // float offset of the layer's bias (N entries)
+  int s_off;     // split form: byte offset of the layer's [3 x N][K] image (terms side by side) in shared memory
 };
 
 struct TcArgs {
@@ -204,7 +205,11 @@ __device__ __forceinline__ void gather_tile_16(const TcArgs& a, long long S, lon
 // Issues one layer's MMA chain (thread 0) and waits for it (all threads).
 // With TERMS = 3 the A tile and the weight images are three BF16 terms each
 // and the chain sums the six products whose term indices add up to at most 2
-// (FP32-grade products).  With `save`, thread 0 also copies the layer's input
+// (FP32-grade products) in four MMAs per 16 columns of K: A0 and A1 against
+// the weight terms [W0|W1] side by side (N = 2N), A0 x W2 into columns
+// N..2N-1 and A2 x W0 into columns 0..N-1; the layer's output is the sum of
+// the two column blocks (acc_row / acc_row4).  A tcgen05.mma costs about the
+// same at N = 2N as at N, so this is two MMAs fewer per K step.  With `save`, thread 0 also copies the layer's input
 // tile (the A operand, 256 * K bytes; with TERMS = 3 the [128][2K] tile of its
 // first two terms, a two-term split of the same values) to global memory by a
 // bulk async copy and, before the caller's barrier lets anyone overwrite A,
@@ -213,26 +218,35 @@ template <int BF16, int TERMS>
 __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, uint32_t wterm, const uint8_t* sA,
                                          uint32_t tstride, uint32_t tmem, uint64_t* bar, uint32_t& phase,
                                          uint8_t* save = nullptr) {
-  constexpr int NP = TERMS == 1 ? 1 : 6;
-  constexpr int PA[6] = {0, 0, 1, 0, 2, 1};  // term of A, per product
-  constexpr int PB[6] = {0, 1, 0, 2, 0, 1};  // term of B
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
     if (save != nullptr) {
       tc::bulk_store(save, sA, (uint32_t)L.K * 256u * (TERMS > 1 ? 2u : 1u));
       tc::bulk_commit();
     }
-    const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
     const uint32_t sbo = (uint32_t)(L.K / 8) * 128;
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-      // A term PA[p] (a_term's layout): terms 0 and 1 are K-column slices of the [128][2K] tile
-      const bool wide = TERMS > 1 && PA[p] < 2;
-      const uint32_t a0 = tc::smem_u32(wide ? sA + PA[p] * (L.K / 8) * 128 : sA + (TERMS > 1 ? 2 * tstride : 0));
-      const uint32_t b0 = tc::smem_u32(sB + PB[p] * wterm + L.b_off);
+    if constexpr (TERMS == 1) {
+      const uint32_t idesc = tc::idesc_f16(128, L.N, BF16);
+      const uint32_t a0 = tc::smem_u32(sA), b0 = tc::smem_u32(sB + L.b_off);
       for (int k = 0; k < L.K / 16; ++k)
-        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, wide ? 2 * sbo : sbo), tc::smem_desc(b0 + k * 256, 128, sbo),
-                    idesc, (p > 0 || k > 0) ? 1u : 0u);
+        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
+                    k > 0 ? 1u : 0u);
+    } else {
+      // A terms (a_term's layout): 0 and 1 are K-column slices of the [128][2K] tile, 2 its own tile
+      const uint64_t a0 = tc::smem_desc(tc::smem_u32(sA), 128, 2 * sbo);
+      const uint64_t a1 = tc::desc_plus(a0, (uint32_t)(L.K / 8) * 128);
+      const uint64_t a2 = tc::smem_desc(tc::smem_u32(sA + 2 * tstride), 128, sbo);
+      // weights [W0|W1|W2] along N (rows): [W0|W1] is the first 2N rows, W0 the first N
+      const uint64_t b01 = tc::smem_desc(tc::smem_u32(sB + L.s_off), 128, sbo);
+      const uint64_t b2 = tc::desc_plus(b01, (uint32_t)(2 * L.N * L.K * 2));
+      const uint32_t i2 = tc::idesc_f16(128, 2 * L.N, 1), i1 = tc::idesc_f16(128, L.N, 1);
+      for (int k = 0; k < L.K / 16; ++k) {
+        const uint32_t o = (uint32_t)k * 256;
+        tc::mma_f16(tmem, tc::desc_plus(a0, o), tc::desc_plus(b01, o), i2, k > 0 ? 1u : 0u);
+        tc::mma_f16(tmem, tc::desc_plus(a1, o), tc::desc_plus(b01, o), i2, 1u);
+        tc::mma_f16(tmem + L.N, tc::desc_plus(a0, o), tc::desc_plus(b2, o), i1, 1u);
+        tc::mma_f16(tmem, tc::desc_plus(a2, o), tc::desc_plus(b01, o), i1, 1u);
+      }
     }
     tc::mma_commit(bar);
   }
@@ -243,12 +257,49 @@ __device__ __forceinline__ bool tc_layer(const TcLayer& L, const uint8_t* sB, ui
   return done;
 }
 
-// Writes 32 values (columns c0..c0+31 of the next layer's input) of row t,
+// Epilogue columns per pass: 32, or 16 for the split form, whose rows are the
+// sum of two TMEM column blocks (registers: its kernel runs 4 CTAs per SM).
+template <int TERMS>
+constexpr int EPI_COLS = TERMS == 1 ? 32 : 16;
+
+// This thread's row of a layer's output, EPI_COLS columns from taddr; with
+// TERMS = 3 the sum of tc_layer's two column blocks (the second n columns on).
+template <int TERMS>
+__device__ __forceinline__ void acc_row(uint32_t taddr, int n, float* v) {
+  if constexpr (TERMS == 1) {
+    tc::ld_32x32b_x32(taddr, v);
+    tc::ld_wait();
+  } else {
+    float u[16];
+    tc::ld_32x32b_x16(taddr, v);
+    tc::ld_32x32b_x16(taddr + n, u);
+    tc::ld_wait();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] += u[i];
+  }
+}
+
+// Same for 4 columns.
+template <int TERMS>
+__device__ __forceinline__ void acc_row4(uint32_t taddr, int n, float* v) {
+  tc::ld_32x32b_x4(taddr, v);
+  if constexpr (TERMS > 1) {
+    float u[4];
+    tc::ld_32x32b_x4(taddr + n, u);
+    tc::ld_wait();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] += u[i];
+  } else {
+    tc::ld_wait();
+  }
+}
+
+// Writes EPI_COLS values (columns c0.. of the next layer's input) of row t,
 // as TERMS operand terms (a_term's layout).
 template <int BF16, int TERMS>
-__device__ __forceinline__ void store_row32(uint8_t* sA, uint32_t tstride, int t, int c0, int K, const float* v) {
+__device__ __forceinline__ void store_row(uint8_t* sA, uint32_t tstride, int t, int c0, int K, const float* v) {
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < EPI_COLS<TERMS> / 8; ++j) {
     if constexpr (TERMS == 1) {
       uint4 w;
       w.x = tc::pack2<BF16>(v[8 * j + 0], v[8 * j + 1]);
@@ -292,8 +343,22 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
   uint64_t* bar = reinterpret_cast<uint64_t*>(sA + TERMS * TSTRIDE);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
   const int t = threadIdx.x, warp = t >> 5;
-  for (int i = t; i < TERMS * a.wbytes / 16; i += 128)
-    reinterpret_cast<uint4*>(sB)[i] = __ldg(reinterpret_cast<const uint4*>(a.wblob) + i);
+  if constexpr (TERMS == 1) {
+    for (int i = t; i < a.wbytes / 16; i += 128)
+      reinterpret_cast<uint4*>(sB)[i] = __ldg(reinterpret_cast<const uint4*>(a.wblob) + i);
+  } else {
+    // the images regrouped layer by layer, the three terms side by side along N
+#pragma unroll 1
+    for (int l = 0; l < D1 + 3; ++l) {
+      const TcLayer& L = a.L[l];
+      const int img16 = L.N * L.K * 2 / 16;
+      for (int i = t; i < 3 * img16; i += 128) {
+        const int j = i / img16, o = i % img16;
+        reinterpret_cast<uint4*>(sB + L.s_off)[i] =
+            __ldg(reinterpret_cast<const uint4*>(a.wblob + (size_t)j * a.wbytes + L.b_off) + o);
+      }
+    }
+  }
   for (int i = t; i < a.nbias; i += 128) sBias[i] = __ldg(a.bias + i);
   if (t == 0) {
     tc::mbar_init(bar, 1);
@@ -335,12 +400,11 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
       ok = __syncthreads_and(ok);
       if (!ok) break;
 #pragma unroll
-      for (int c0 = 0; c0 < W; c0 += 32) {
-        tc::ld_32x32b_x32(trow + c0, v);
-        tc::ld_wait();
+      for (int c0 = 0; c0 < W; c0 += EPI_COLS<TERMS>) {
+        acc_row<TERMS>(trow + c0, a.L[l].N, v);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + sBias[a.L[l].bias_off + c0 + i], 0.f);
-        store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
+        for (int i = 0; i < EPI_COLS<TERMS>; ++i) v[i] = fmaxf(v[i] + sBias[a.L[l].bias_off + c0 + i], 0.f);
+        store_row<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
       }
       sync_for_mma();
     }
@@ -351,17 +415,15 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
     float sigma;
     {
       float sv[4];
-      tc::ld_32x32b_x4(trow + W, sv);
-      tc::ld_wait();
+      acc_row4<TERMS>(trow + W, a.L[D1].N, sv);
       sigma = sv[0] + sBias[a.L[D1].bias_off + W];
     }
 #pragma unroll
-    for (int c0 = 0; c0 < W; c0 += 32) {
-      tc::ld_32x32b_x32(trow + c0, v);
-      tc::ld_wait();
+    for (int c0 = 0; c0 < W; c0 += EPI_COLS<TERMS>) {
+      acc_row<TERMS>(trow + c0, a.L[D1].N, v);
 #pragma unroll
-      for (int i = 0; i < 32; ++i) v[i] += sBias[a.L[D1].bias_off + c0 + i];
-      store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
+      for (int i = 0; i < EPI_COLS<TERMS>; ++i) v[i] += sBias[a.L[D1].bias_off + c0 + i];
+      store_row<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
     }
     sync_for_mma();
     // mlp2 first layer: relu(hidden W^T + per-ray (bias + PE term))
@@ -372,18 +434,17 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
       const int ray = valid ? __ldg(a.seg_ray + s) : 0;
       const float4* po = reinterpret_cast<const float4*>(a.pe_out + (long long)ray * W);
 #pragma unroll
-      for (int c0 = 0; c0 < W; c0 += 32) {
-        tc::ld_32x32b_x32(trow + c0, v);
-        tc::ld_wait();
+      for (int c0 = 0; c0 < W; c0 += EPI_COLS<TERMS>) {
+        acc_row<TERMS>(trow + c0, a.L[D1 + 1].N, v);
 #pragma unroll
-        for (int i = 0; i < 32; i += 4) {
+        for (int i = 0; i < EPI_COLS<TERMS>; i += 4) {
           const float4 p = __ldg(po + (c0 + i) / 4);
           v[i] = fmaxf(v[i] + p.x, 0.f);
           v[i + 1] = fmaxf(v[i + 1] + p.y, 0.f);
           v[i + 2] = fmaxf(v[i + 2] + p.z, 0.f);
           v[i + 3] = fmaxf(v[i + 3] + p.w, 0.f);
         }
-        store_row32<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
+        store_row<BF16, TERMS>(sA, TSTRIDE, t, c0, W, v);
       }
     }
     sync_for_mma();
@@ -394,8 +455,7 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
     if (!ok) break;
     {
       float o[4];
-      tc::ld_32x32b_x4(trow, o);
-      tc::ld_wait();
+      acc_row4<TERMS>(trow, a.L[D1 + 2].N, o);
       const int bo = a.L[D1 + 2].bias_off;
       if (valid)
         a.out4[s] = make_float4(sigma, sigmoidf_acc(o[0] + sBias[bo]), sigmoidf_acc(o[1] + sBias[bo + 1]),
@@ -417,7 +477,8 @@ __global__ void __launch_bounds__(128, TERMS == 1 ? 8 : ((C == 32 && W == 32) ? 
 // kernels that allocate TMEM).
 template <int C, int W, int D1, int BF16, int TERMS = 1>
 int launch_decode_fwd_tc(const TcArgs& a, cudaStream_t st) {
-  constexpr int NCOLS = W == 32 ? 64 : 128;
+  // split form: two column blocks of the widest N
+  constexpr int NCOLS = TERMS > 1 ? (W == 32 ? 128 : 256) : (W == 32 ? 64 : 128);
   constexpr int KMAX = C > W ? C : W;
   const size_t smem = (size_t)TERMS * a.wbytes + (size_t)a.nbias * 4 + (size_t)TERMS * 128 * KMAX * 2 + 16;
   auto k = decode_fwd_tc<C, W, D1, BF16, NCOLS, TERMS>;
@@ -528,6 +589,15 @@ static int decode_fwd_tc_args(TcArgs& a, int kind, int channels, int terms, cons
     DV_CHECK(L.K % 16 == 0 && L.N % 16 == 0 && L.N >= 16 && L.N <= 256 && L.b_off % 16 == 0, DV_ERR_ARG);
     DV_CHECK((long long)L.b_off + (long long)L.N * L.K * 2 <= wbytes && L.bias_off + L.N <= nbias, DV_ERR_ARG);
     DV_CHECK(L.N <= (W == 32 ? 64 : 128), DV_ERR_ARG);
+  }
+  // the split form's images regrouped in shared memory, layer by layer
+  {
+    long long off = 0;
+    for (int l = 0; l < n_layers; ++l) {
+      a.L[l].s_off = (int)off;
+      off += 3LL * a.L[l].N * a.L[l].K * 2;
+    }
+    DV_CHECK(terms == 1 || off <= 3LL * wbytes, DV_ERR_ARG);
   }
   // saved layer inputs: one record of sum(256 K) bytes (per saved term) per 128-segment tile
   if (save != nullptr) {
