@@ -41,11 +41,11 @@
 // r = t % 128 (TMEM lane r; warps w and w + 4 share a lane quadrant) and half
 // h = t / 128 of each row's columns in the epilogues; lane 0 of warp 8 issues
 // the MMAs and the record loads.  The scatter of a tile's feature gradient
-// into the grid runs on the chain threads while the next tile's MMAs run.  Shared memory (about 184 KiB):
-// the propagation images, the saved record in five per-layer slots, the PE
-// tile, the delta tile, a tile of ones and the FP32 staging rows of the
-// feature gradient.  TMEM: all 512 columns (64 working, 384 weight-gradient
-// and 64 bias-gradient columns).
+// into the grid runs on the chain threads while the next tile's MMAs run.
+// Shared memory (about 184 KiB): the propagation images, the saved record in
+// five per-layer slots, the PE tile, the delta tile, a tile of ones and the
+// FP32 staging rows of the feature gradient.  TMEM: all 512 columns (64
+// working, 384 weight-gradient and 64 bias-gradient columns).
 // Reference semantics: the autograd backward of model/diver.py:159-180.
 #include "common.cuh"
 #include "integrate.cuh"
