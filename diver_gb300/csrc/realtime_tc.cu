@@ -34,7 +34,8 @@ namespace dv {
 namespace rtc {
 
 // Tensor-core images of the folded layers, [N][K] in the K-major core-matrix
-// layout, one term (three terms follow each other, TERM bytes apart):
+// layout; per layer its three terms side by side along N (term j in rows
+// jN..jN+N-1, S bytes each), layers one after the other:
 //   B0 [W][32]      L0 (32 -> W)
 //   B1 [W + 16][W]  rows 0..W-1 the hidden part of mlp2's first layer, row W
 //                   the sigma weights, the rest zero
@@ -42,8 +43,9 @@ namespace rtc {
 template <int W>
 struct Img {
   static constexpr int n0 = W, k0 = 32, n1 = W + 16, k1 = W, n2 = 16, k2 = W;
-  static constexpr int off0 = 0, off1 = off0 + n0 * k0 * 2, off2 = off1 + n1 * k1 * 2;
-  static constexpr int TERM = off2 + n2 * k2 * 2;
+  static constexpr int s0 = n0 * k0 * 2, s1 = n1 * k1 * 2, s2 = n2 * k2 * 2;  // one term of each layer
+  static constexpr int off0 = 0, off1 = off0 + 3 * s0, off2 = off1 + 3 * s1;
+  static constexpr int TERM = s0 + s1 + s2;  // one term of all layers (the blob holds three)
   static constexpr int ELEMS = n0 * k0 + n1 * k1 + n2 * k2;
 };
 
@@ -53,13 +55,14 @@ __global__ void tc_pack_kernel(const float* __restrict__ packed, uint8_t* __rest
   using I = Img<W>;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= I::ELEMS) return;
-  int n, k, K, off;
+  int n, k, K, off, sz;
   float x;
   if (e < I::n0 * I::k0) {
     n = e / I::k0;
     k = e % I::k0;
     K = I::k0;
     off = I::off0;
+    sz = I::s0;
     x = packed[L::l0_w + k * W + n];
   } else if (e < I::n0 * I::k0 + I::n1 * I::k1) {
     const int f = e - I::n0 * I::k0;
@@ -67,6 +70,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ packed, uint8_t* __rest
     k = f % I::k1;
     K = I::k1;
     off = I::off1;
+    sz = I::s1;
     x = n < W ? packed[L::l2_w + k * W + n] : (n == W ? packed[L::sig + k] : 0.f);
   } else {
     const int f = e - I::n0 * I::k0 - I::n1 * I::k1;
@@ -74,6 +78,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ packed, uint8_t* __rest
     k = f % I::k2;
     K = I::k2;
     off = I::off2;
+    sz = I::s2;
     x = n < 3 ? packed[L::l3_w + k * 4 + n] : 0.f;
   }
   const uint32_t o = off + tc::kmajor_offset(n, k, K);
@@ -81,7 +86,7 @@ __global__ void tc_pack_kernel(const float* __restrict__ packed, uint8_t* __rest
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     const __nv_bfloat16 b = __float2bfloat16_rn(r);
-    *reinterpret_cast<__nv_bfloat16*>(blob + i * I::TERM + o) = b;
+    *reinterpret_cast<__nv_bfloat16*>(blob + i * sz + o) = b;
     r = __fsub_rn(r, __bfloat162float(b));
   }
 }
@@ -102,24 +107,30 @@ struct Args {
 
 __device__ __forceinline__ int clampi(int x, int hi) { return x < 0 ? 0 : (x > hi ? hi : x); }
 
-// One layer: D[128][N] = A[128][K] x B^T with three-term operands, six
-// products (thread 0 issues, every thread waits).
-template <int K, int N, int TERM>
+// One layer with three-term operands: the six products whose term indices
+// add up to at most 2 as four MMAs per 16 columns of K (thread 0 issues, every
+// thread waits): A0 and A1 against [B0|B1] (N = 2N) into columns 0..2N-1,
+// A0 x B2 into N..2N-1 and A2 x B0 into 0..N-1.  The layer's output is the sum
+// of the two column blocks (row16 / row4).
+template <int K, int N>
 __device__ __forceinline__ bool tc_layer3(const uint8_t* sA, uint32_t tstride, const uint8_t* sB, int boff,
                                           uint32_t tmem, uint64_t* bar, uint32_t& phase) {
-  constexpr int PA[6] = {0, 0, 1, 0, 2, 1};
-  constexpr int PB[6] = {0, 1, 0, 2, 0, 1};
   if (threadIdx.x == 0) {
     tc::fence_after_sync();
-    const uint32_t idesc = tc::idesc_f16(128, N, 1);
     constexpr uint32_t sbo = (K / 8) * 128;
+    const uint32_t i2 = tc::idesc_f16(128, 2 * N, 1), i1 = tc::idesc_f16(128, N, 1);
+    const uint64_t a0 = tc::smem_desc(tc::smem_u32(sA), 128, sbo);
+    const uint64_t a1 = tc::smem_desc(tc::smem_u32(sA + tstride), 128, sbo);
+    const uint64_t a2 = tc::smem_desc(tc::smem_u32(sA + 2 * tstride), 128, sbo);
+    const uint64_t b01 = tc::smem_desc(tc::smem_u32(sB + boff), 128, sbo);
+    const uint64_t b2 = tc::desc_plus(b01, 2 * N * K * 2);
 #pragma unroll
-    for (int p = 0; p < 6; ++p) {
-      const uint32_t a0 = tc::smem_u32(sA + PA[p] * tstride), b0 = tc::smem_u32(sB + PB[p] * TERM + boff);
-#pragma unroll
-      for (int k = 0; k < K / 16; ++k)
-        tc::mma_f16(tmem, tc::smem_desc(a0 + k * 256, 128, sbo), tc::smem_desc(b0 + k * 256, 128, sbo), idesc,
-                    (p > 0 || k > 0) ? 1u : 0u);
+    for (int k = 0; k < K / 16; ++k) {
+      const uint32_t o = k * 256;
+      tc::mma_f16(tmem, tc::desc_plus(a0, o), tc::desc_plus(b01, o), i2, k > 0 ? 1u : 0u);
+      tc::mma_f16(tmem, tc::desc_plus(a1, o), tc::desc_plus(b01, o), i2, 1u);
+      tc::mma_f16(tmem + N, tc::desc_plus(a0, o), tc::desc_plus(b2, o), i1, 1u);
+      tc::mma_f16(tmem, tc::desc_plus(a2, o), tc::desc_plus(b01, o), i1, 1u);
     }
     tc::mma_commit(bar);
   }
@@ -127,6 +138,26 @@ __device__ __forceinline__ bool tc_layer3(const uint8_t* sA, uint32_t tstride, c
   if (done) phase ^= 1u;
   tc::fence_after_sync();
   return done;
+}
+
+// This thread's row of a layer's output: 16 columns from taddr plus the same
+// columns of the second block n columns on (tc_layer3's two blocks).
+__device__ __forceinline__ void row16(uint32_t taddr, int n, float* v) {
+  float u[16];
+  tc::ld_32x32b_x16(taddr, v);
+  tc::ld_32x32b_x16(taddr + n, u);
+  tc::ld_wait();
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] += u[i];
+}
+
+__device__ __forceinline__ void row4(uint32_t taddr, int n, float* v) {
+  float u[4];
+  tc::ld_32x32b_x4(taddr, v);
+  tc::ld_32x32b_x4(taddr + n, u);
+  tc::ld_wait();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] += u[i];
 }
 
 // Writes n values (multiple of 8) of row t as three BF16 terms of a K-major tile with K columns.
@@ -285,47 +316,43 @@ __global__ void __launch_bounds__(128, W == 32 ? 4 : 1) mlp_eval_tc_kernel(const
       integrate_tile<FIRST>(a, sHit, sb + Bi::b_in, sA, TSTRIDE);
       sync_for_mma();
       // L0: h1 = W0 x + b0, relu
-      ok = __syncthreads_and(tc_layer3<32, W, I::TERM>(sA, TSTRIDE, sB, I::off0, tmem, bar, phase));
+      ok = __syncthreads_and(tc_layer3<32, W>(sA, TSTRIDE, sB, I::off0, tmem, bar, phase));
       if (!ok) break;
       {
-        float v[32];
+        float v[16];
 #pragma unroll
-        for (int c0 = 0; c0 < W; c0 += 32) {
-          tc::ld_32x32b_x32(trow + c0, v);
-          tc::ld_wait();
+        for (int c0 = 0; c0 < W; c0 += 16) {
+          row16(trow + c0, I::n0, v);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + sb[Bi::l0_b + c0 + i], 0.f);
-          put_row3<W, 32>(sA + tc::kmajor_offset(0, c0, W), TSTRIDE, t, v);
+          for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + sb[Bi::l0_b + c0 + i], 0.f);
+          put_row3<W, 16>(sA + tc::kmajor_offset(0, c0, W), TSTRIDE, t, v);
         }
       }
       sync_for_mma();
       // L1: h2 (+ pixel constant) and sigma
-      ok = __syncthreads_and(tc_layer3<W, W + 16, I::TERM>(sA, TSTRIDE, sB, I::off1, tmem, bar, phase));
+      ok = __syncthreads_and(tc_layer3<W, W + 16>(sA, TSTRIDE, sB, I::off1, tmem, bar, phase));
       if (!ok) break;
       float alpha;
       {
         float sv[4];
-        tc::ld_32x32b_x4(trow + W, sv);
-        tc::ld_wait();
+        row4(trow + W, I::n1, sv);
         alpha = 1.f - expf(-fmaxf(sv[0] + sb[Bi::sig_b], 0.f));
-        float v[32];
+        float v[16];
 #pragma unroll
-        for (int c0 = 0; c0 < W; c0 += 32) {
-          tc::ld_32x32b_x32(trow + c0, v);
-          tc::ld_wait();
+        for (int c0 = 0; c0 < W; c0 += 16) {
+          row16(trow + c0, I::n1, v);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + pe2[c0 + i], 0.f);
-          put_row3<W, 32>(sA + tc::kmajor_offset(0, c0, W), TSTRIDE, t, v);
+          for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + pe2[c0 + i], 0.f);
+          put_row3<W, 16>(sA + tc::kmajor_offset(0, c0, W), TSTRIDE, t, v);
         }
       }
       sync_for_mma();
       // L2: colour logits, sigmoid, compositing (skip alpha < 1e-2, stop at T < 1e-2)
-      ok = __syncthreads_and(tc_layer3<W, 16, I::TERM>(sA, TSTRIDE, sB, I::off2, tmem, bar, phase));
+      ok = __syncthreads_and(tc_layer3<W, 16>(sA, TSTRIDE, sB, I::off2, tmem, bar, phase));
       if (!ok) break;
       {
         float o[4];
-        tc::ld_32x32b_x4(trow, o);
-        tc::ld_wait();
+        row4(trow, I::n2, o);
         if (hit && !(alpha < 1e-2f)) {
           const float wgt = acc.w * alpha;
           acc.x += wgt * sigmoidf_acc(o[0] + sb[Bi::l3_b]);
@@ -357,7 +384,7 @@ __global__ void __launch_bounds__(128, W == 32 ? 4 : 1) mlp_eval_tc_kernel(const
 template <int W, int FIRST>
 int launch(const Args& a, cudaStream_t st) {
   using I = Img<W>;
-  constexpr int NCOLS = W == 32 ? 64 : 128;
+  constexpr int NCOLS = W == 32 ? 128 : 256;  // two column blocks of the widest layer (W + 16)
   constexpr int KMAX = W > 32 ? W : 32;
   const size_t smem = 3 * (size_t)I::TERM + 3 * (size_t)128 * KMAX * 2 + (size_t)(Bias<W>::size + 3) / 4 * 16 +
                       128 * 8 * 4 + 16;
