@@ -87,9 +87,9 @@ def alg_work(kernel, S, U, R):
 TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52, "dv_decode_fwd_tc_split": 992.6}
 # Kernels of this library per captured training step: row clear, three weight
 # image gathers, ray PE, slot walk, 3 scan kernels, slot compaction, decoder
-# forward, compositing forward, compositing backward, row marking, decoder
-# backward.
-OUR_LAUNCHES_PER_STEP = 15
+# forward, compositing forward, sparsity mean, loss, loss gradients,
+# compositing backward, row marking, decoder backward.
+OUR_LAUNCHES_PER_STEP = 18
 
 
 def parse():
@@ -309,8 +309,10 @@ def unique_corner_rows(seg, n):
 def train_step(field, o, d, tgt, form="fp32"):
     import torch
 
+    from diver_gb300.renderer import l2_loss
+
     rgb, reg = field(o, d, form=form)
-    loss = torch.nn.functional.mse_loss(rgb, tgt) + L_S * reg
+    loss = l2_loss(rgb, reg, tgt, L_S)
     gv, gp = torch.autograd.grad(loss, [field.voxels, field.params])
     return loss, gv, gp
 

@@ -53,6 +53,9 @@ SIGNATURES = {
     "dv_decode_fwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P]),
     "dv_composite_fwd": (I32, [I32, P, P, I32, P, P, P, P]),
     "dv_composite_bwd": (I32, [I32, P, P, P, P, F32, P, P, P]),
+    "dv_reg_mean": (I32, [I32, P, P, F32, P, P, P]),
+    "dv_l2_loss_fwd": (I32, [I64, P, P, P, F32, P, P]),
+    "dv_l2_loss_bwd": (I32, [I64, P, P, P, F32, P, P, P]),
     "dv_occupancy_max": (I32, [I32, P, P, P, I32, I32, P, P]),
     "dv_decode_bwd": (I32, [I32, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, P, P, P]),
     "dv_decode_fwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, I32, P, P, I32, I32, I32, P, P, I64, P, P, P, P, I64, P,

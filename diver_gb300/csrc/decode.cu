@@ -164,6 +164,60 @@ static int sm_count() {
   return n > 0 ? n : 1;
 }
 
+// Sum over the 1024 threads of a block (tree through shared memory); every
+// thread gets the total.
+__device__ __forceinline__ float block_sum_1024(float v) {
+  __shared__ float part[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) part[w] = v;
+  __syncthreads();
+  v = part[lane];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// The sparsity term's mean over the padded [B, M] (model/diver.py:199-205:
+// the per-ray sums divided by B * M, M the longest ray, at least 1), M read on
+// the device when m_dev is given; inv_m = 1 / M for the backward.  One block.
+__global__ void __launch_bounds__(1024) reg_mean_kernel(const float* __restrict__ reg, int B, const int* m_dev,
+                                                        float m_host, float* out, float* inv_m) {
+  float v = 0.f;
+  for (int i = threadIdx.x; i < B; i += 1024) v += reg[i];
+  v = block_sum_1024(v);
+  if (threadIdx.x == 0) {
+    const float m = fmaxf(m_dev ? (float)*m_dev : m_host, 1.f);
+    out[0] = v / ((float)B * m);
+    inv_m[0] = 1.f / m;
+  }
+}
+
+// Training loss of train.py:84-85,109-113: mean((x - y)^2) over n values plus
+// l_s times the sparsity term (a device scalar, or none).  One block.
+__global__ void __launch_bounds__(1024) l2_loss_fwd_kernel(const float* __restrict__ x, const float* __restrict__ y,
+                                                           long long n, const float* reg, float l_s, float* loss) {
+  float v = 0.f;
+  for (long long i = threadIdx.x; i < n; i += 1024) {
+    const float d = x[i] - y[i];
+    v = fmaf(d, d, v);
+  }
+  v = block_sum_1024(v);
+  if (threadIdx.x == 0) loss[0] = v / (float)n + (reg ? l_s * reg[0] : 0.f);
+}
+
+// Its gradients for the incoming dL (a device scalar): dx = 2 (x - y) / n * dL,
+// dreg = l_s * dL.
+__global__ void l2_loss_bwd_kernel(const float* __restrict__ x, const float* __restrict__ y, long long n,
+                                   const float* g, float l_s, float* dx, float* dreg) {
+  const float gg = g[0];
+  const float c = 2.f * gg / (float)n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dx[i] = c * (x[i] - y[i]);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && dreg) dreg[0] = l_s * gg;
+}
+
 }  // namespace dv
 
 using namespace dv;
@@ -345,6 +399,31 @@ int dv_decode_bwd(int kind, int channels, const float* params, const float* voxe
   if (kind == 64 && channels == 32) return decode_bwd_v64c32(a, st, sms);
   if (kind == 64 && channels == 64) return decode_bwd_v64c64(a, st, sms);
   return DV_ERR_UNSUPPORTED;
+}
+
+int dv_reg_mean(int batch, const float* reg, const int* max_dev, float max_host, float* mean, float* inv_max,
+                void* stream) {
+  DV_CHECK(batch >= 0 && reg && mean && inv_max, DV_ERR_ARG);
+  reg_mean_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(reg, batch, max_dev, max_host, mean, inv_max);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_l2_loss_fwd(long long n, const float* x, const float* y, const float* reg, float l_s, float* loss,
+                   void* stream) {
+  DV_CHECK(n > 0 && x && y && loss, DV_ERR_ARG);
+  l2_loss_fwd_kernel<<<1, 1024, 0, (cudaStream_t)stream>>>(x, y, n, reg, l_s, loss);
+  DV_TRY_LAUNCH();
+  return DV_OK;
+}
+
+int dv_l2_loss_bwd(long long n, const float* x, const float* y, const float* grad, float l_s, float* dx, float* dreg,
+                   void* stream) {
+  DV_CHECK(n > 0 && x && y && grad && dx, DV_ERR_ARG);
+  const long long blocks = std::min<long long>((n + 255) / 256, 4LL * 152);
+  l2_loss_bwd_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(x, y, n, grad, l_s, dx, dreg);
+  DV_TRY_LAUNCH();
+  return DV_OK;
 }
 
 }  // extern "C"

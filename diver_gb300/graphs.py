@@ -30,7 +30,7 @@ from __future__ import annotations
 import torch
 
 from . import _native as N
-from .renderer import DIVeRField, _grid
+from .renderer import DIVeRField, _grid, l2_loss
 
 
 def _warm_and_capture(fn, warmup: int):
@@ -82,7 +82,7 @@ class TrainStepGraph:
             filled.record()
         rgb, reg = f(self.o, self.d, form=self.form, capacity=self.capacity,
                      grad_voxels=(self._grid_grad, filled, self._touched))
-        loss = torch.nn.functional.mse_loss(rgb, self.target) + self.l_s * reg
+        loss = l2_loss(rgb, reg, self.target, self.l_s)
         gv, gp = torch.autograd.grad(loss, [f.voxels, f.params])
         return loss.detach(), gv, gp
 

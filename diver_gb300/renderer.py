@@ -199,12 +199,13 @@ class SegmentRender(Function):
                N.ptr(reg), st)
         # mean over the padded [B, M]; M (max segments per ray) stays on the
         # device when the segments were built without a host read
-        M = seg.max_count if seg.max_count is not None else seg.max_dev.clamp_min(1).float()
-        if not isinstance(M, torch.Tensor):
-            M = float(max(M, 1))
-        reg_mean = reg.sum() / (float(B) * M)
+        reg_mean = torch.empty((), device=dev)
+        inv_m = torch.empty(1, device=dev)
+        on_dev = seg.max_count is None
+        _timed("dv_reg_mean", B, N.ptr(reg), N.ptr(seg.max_dev) if on_dev else None,
+               0.0 if on_dev else float(seg.max_count), N.ptr(reg_mean), N.ptr(inv_m), st)
         ctx.save_for_backward(voxels, params, dirs, pe_feat, pe_out, out4, rgb)
-        ctx.seg, ctx.kind, ctx.M, ctx.tc, ctx.grad_voxels = seg, kind, M, tc, grad_voxels
+        ctx.seg, ctx.kind, ctx.inv_m, ctx.tc, ctx.grad_voxels = seg, kind, inv_m, tc, grad_voxels
         return rgb, reg_mean
 
     @staticmethod
@@ -220,7 +221,7 @@ class SegmentRender(Function):
         # as a device scalar (no host read of either)
         scale = None
         if g_reg is not None:
-            scale = (g_reg.detach().float().reshape(1) / ctx.M).reshape(1).contiguous()
+            scale = (g_reg.detach().float().reshape(1) * ctx.inv_m).contiguous()
         d4 = torch.empty_like(out4)
         _timed("dv_composite_bwd", B, N.ptr(seg.offsets), N.ptr(out4), N.ptr(rgb), N.ptr(g_rgb),
                1.0 / B if scale is not None else 0.0, N.ptr(scale), N.ptr(d4), st)
@@ -242,6 +243,42 @@ class SegmentRender(Function):
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)
         return gv, gp, None, None, None, None, None, None, None, None, None
+
+
+class L2Loss(Function):
+    """mse(rgb, target) + l_s * reg (train.py:84-85,109-113) as one launch
+    forward (dv_l2_loss_fwd) and one backward (dv_l2_loss_bwd)."""
+
+    @staticmethod
+    def forward(ctx, rgb, reg, target, l_s: float):
+        dev = rgb.device
+        loss = torch.empty((), device=dev)
+        _timed("dv_l2_loss_fwd", rgb.numel(), N.ptr(rgb), N.ptr(target), N.ptr(reg), l_s, N.ptr(loss),
+               N.stream(dev))
+        ctx.save_for_backward(rgb, target)
+        ctx.l_s = l_s
+        return loss
+
+    @staticmethod
+    def backward(ctx, g):
+        rgb, target = ctx.saved_tensors
+        d_rgb = torch.empty_like(rgb)
+        d_reg = torch.empty((), device=rgb.device)
+        g = g.detach().float().contiguous()
+        _timed("dv_l2_loss_bwd", rgb.numel(), N.ptr(rgb), N.ptr(target), N.ptr(g), ctx.l_s, N.ptr(d_rgb),
+               N.ptr(d_reg), N.stream(rgb.device))
+        return d_rgb, d_reg, None, None
+
+
+def l2_loss(rgb: torch.Tensor, reg: torch.Tensor, target: torch.Tensor, l_s: float) -> torch.Tensor:
+    """The training loss mean((rgb - target)^2) + l_s * reg of a render (reg:
+    the sparsity term, a 0-d tensor), differentiable in rgb and reg."""
+    N.need_cuda("rgb", rgb, torch.float32)
+    N.need_cuda("target", target, torch.float32)
+    N.need_cuda("reg", reg, torch.float32)
+    if target.shape != rgb.shape or reg.numel() != 1:
+        raise ValueError("target must match rgb and reg must be a single value")
+    return L2Loss.apply(rgb, reg, target, float(l_s))
 
 
 def render_segments(voxels, params, seg: Segments, dirs, kind="diver32", white_back=True, tc: TcWeights | None = None,

@@ -270,6 +270,22 @@ DV_API int dv_composite_bwd(int batch, const int64_t* offsets, const float* out4
                             const float* grad_rgb, float reg_coef, const float* reg_scale, float* d4,
                             void* stream);
 
+/* The sparsity term's mean (model/diver.py:199-205): mean[0] = sum(reg[0..batch))
+ * / (batch * M), M = max(*max_dev, 1) when max_dev is given (the longest ray,
+ * kept on the device), else max(max_host, 1); inv_max[0] = 1 / M for the
+ * backward's dv_composite_bwd reg_scale.  One launch, no host read. */
+DV_API int dv_reg_mean(int batch, const float* reg, const int* max_dev, float max_host, float* mean,
+                       float* inv_max, void* stream);
+
+/* The training loss of train.py:84-85,109-113 and its gradients, as one launch
+ * each (no counterpart in the reference, which composes them from torch ops):
+ * loss[0] = mean over n of (x - y)^2 + l_s * reg[0] (reg optional);
+ * dx = 2 (x - y) / n * grad[0], dreg[0] = l_s * grad[0] (dreg optional). */
+DV_API int dv_l2_loss_fwd(long long n, const float* x, const float* y, const float* reg, float l_s, float* loss,
+                          void* stream);
+DV_API int dv_l2_loss_bwd(long long n, const float* x, const float* y, const float* grad, float l_s, float* dx,
+                          float* dreg, void* stream);
+
 /* Accumulates the feature-grid gradient (grad_voxels, same layout as voxels)
  * and the packed parameter gradient (grad_params) of the segments' decode. */
 DV_API int dv_decode_bwd(int kind, int channels, const float* params, const float* voxels, int nvx,
