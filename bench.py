@@ -88,8 +88,9 @@ TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52, "dv_
 # Kernels of this library per captured training step: row clear, three weight
 # image gathers, ray PE, slot walk, 3 scan kernels, slot compaction, decoder
 # forward, compositing forward, sparsity mean, loss, loss gradients,
-# compositing backward, row marking, decoder backward.
-OUR_LAUNCHES_PER_STEP = 18
+# compositing backward, decoder backward (which also marks the rows the next
+# step's clear zeroes).
+OUR_LAUNCHES_PER_STEP = 17
 
 
 def parse():

@@ -66,7 +66,7 @@ SIGNATURES = {
     "dv_decode_tc_split_save_bytes": (I64, [I32, I32, I64]),
     "dv_tc_image": (I32, [P, I64, P, I64, I32, P, P]),
     "dv_decode_bwd_tc_split": (I32, [I32, I32, P, I32, P, I32, I32, I32, I32, P, P, I64, P, P, P, P, I64, P, P, P,
-                                     P, P]),
+                                     P, P, P]),
     "dv_wait_selftest": (I32, [I32, P, P]),
     "dv_decode_bwd_tc": (I32, [I32, I32, I32, P, I32, P, I32, P, P, I32, P, I32, P, I32, I32, I32, P, P, I64, P, P,
                                P, P, P, I64, P, P, P, P, P]),

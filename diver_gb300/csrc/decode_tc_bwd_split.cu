@@ -97,6 +97,7 @@ struct Args {
   const uint8_t* saved;  // RECORD bytes per tile
   float* grad_grid;
   float* grad_params;    // packed torch layout
+  uint8_t* touched;      // optional: a byte per grid row, set at each segment's lower corner
   int w_off[NL], b_off[NL];
   const uint8_t* wb;     // transposed weight images, three terms of wterm bytes
   int wterm;
@@ -264,6 +265,8 @@ struct Scatter {
     for (int i = 0; i < 6; ++i) p[i] = __shfl_sync(0xffffffffu, crd[i], k, C / 4);
     if (s0 + k < S) {
       const SegCorner sc = segment_corners(p[0], p[1], p[2], p[3], p[4], p[5], a.nvx, a.nvy, a.nvz);
+      // the row marks for the next step's sparse clear (dv_mark_corner_rows' rule)
+      if (a.touched && q == 0) a.touched[((long long)sc.z * a.nvy + sc.y) * a.nvx + sc.x] = 1;
       const float4 g = *reinterpret_cast<const float4*>(stage + (ls0 + k) * (C + 4) + 4 * q);
       const bool whole = sc.x1 == sc.x + 1 && sc.y1 == sc.y + 1 && sc.z1 == sc.z + 1;
       int axis = -1;
@@ -619,7 +622,7 @@ int dv_decode_bwd_tc_split(int kind, int channels, const void* wb, int wb_term_b
                            int n_layers, int nvx, int nvy, int nvz, const float* seg, const int* seg_ray,
                            long long n_seg, const int64_t* n_seg_dev, const float* pe_feat, const float* d4,
                            const void* saved, long long saved_bytes, const float* out4, float* grad_voxels,
-                           float* grad_params, int* err, void* stream) {
+                           float* grad_params, unsigned char* touched, int* err, void* stream) {
   using namespace dv::bws;
   DV_CHECK(n_seg >= 0, DV_ERR_ARG);
   DV_CHECK(kind == 32 && channels == 32 && n_layers == NL, DV_ERR_UNSUPPORTED);
@@ -645,6 +648,7 @@ int dv_decode_bwd_tc_split(int kind, int channels, const void* wb, int wb_term_b
   a.saved = reinterpret_cast<const uint8_t*>(saved);
   a.grad_grid = grad_voxels;
   a.grad_params = grad_params;
+  a.touched = touched;
   a.wb = reinterpret_cast<const uint8_t*>(wb);
   a.wterm = wb_term_bytes;
   a.err = err;

@@ -130,11 +130,18 @@ class TcWeights:
         n = int(getattr(N.lib(), fn)(kind, channels, n_seg))
         return torch.empty(max(n, 16), dtype=torch.uint8, device=device)
 
-    def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st, saved=None, out4=None) -> bool:
+    def marks_rows(self, saved) -> bool:
+        """Whether backward() with this save buffer also sets the row marks
+        of dv_mark_corner_rows (the split form does, in its scatter)."""
+        return self.bwd is not None and self.terms > 1 and saved is not None
+
+    def backward(self, kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st, saved=None, out4=None,
+                 touched=None) -> bool:
         """Tensor-core backward (DIVeR32, BF16 / split BF16); False when this
         decoder / form has none (the caller then runs the FP32 CUDA backward).
         With `saved` (the forward's save buffer) and its `out4` the forward is
-        read back instead of recomputed; the split form requires it."""
+        read back instead of recomputed; the split form requires it, and sets
+        the row marks in `touched` when given (marks_rows)."""
         if self.bwd is None or (self.terms > 1 and saved is None):
             return False
         nx, ny, nz, c = _grid(voxels)
@@ -143,7 +150,7 @@ class TcWeights:
             _timed("dv_decode_bwd_tc_split", kind, c, N.ptr(wb), wb.numel() // self.terms, tb.data_ptr(),
                    tb.shape[0], nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray), seg.total, seg.count_ptr,
                    N.ptr(pe_feat), N.ptr(d4), N.ptr(saved), saved.numel(), N.ptr(out4), N.ptr(gv), N.ptr(gp),
-                   N.ptr(self.err), st)
+                   N.ptr(touched), N.ptr(self.err), st)
             return True
         _timed("dv_decode_bwd_tc", kind, c, int(self.bf16), N.ptr(self.blob), self.blob.numel(), N.ptr(self.bias),
                self.bias.numel(), self.table.data_ptr(), N.ptr(wb), wb.numel(), tb.data_ptr(), tb.shape[0],
@@ -230,15 +237,18 @@ class SegmentRender(Function):
             # ran; wait for that, then mark the rows this step writes when the
             # caller clears only those (dv_clear_marked_rows)
             gv, filled, *touched = ctx.grad_voxels
+            touched = touched[0] if touched else None
             torch.cuda.current_stream(dev).wait_event(filled)
-            if touched and touched[0] is not None:
-                N.call("dv_mark_corner_rows", N.ptr(seg.seg), seg.total, seg.count_ptr, nx, ny, nz, N.ptr(touched[0]),
-                       st)
         else:
-            gv = torch.zeros_like(voxels)
+            gv, touched = torch.zeros_like(voxels), None
+        saved = getattr(ctx, "saved_layers", None)
+        # the split tensor-core backward sets the row marks in its scatter
+        if touched is not None and not (ctx.tc is not None and ctx.tc.marks_rows(saved)):
+            N.call("dv_mark_corner_rows", N.ptr(seg.seg), seg.total, seg.count_ptr, nx, ny, nz, N.ptr(touched), st)
+            touched = None
         gp = torch.zeros_like(params)
-        if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st,
-                                                  getattr(ctx, "saved_layers", None), out4):
+        if ctx.tc is not None and ctx.tc.backward(ctx.kind, voxels, seg, pe_feat, pe_out, d4, gv, gp, st, saved, out4,
+                                                  touched):
             return gv, gp, None, None, None, None, None, None, None, None, None
         _timed("dv_decode_bwd", ctx.kind, c, N.ptr(params), N.ptr(voxels), nx, ny, nz, N.ptr(seg.seg), N.ptr(seg.ray),
                seg.total, seg.count_ptr, N.ptr(pe_feat), N.ptr(pe_out), N.ptr(d4), N.ptr(gv), N.ptr(gp), st)

@@ -416,13 +416,15 @@ DV_API int dv_decode_bwd_tc(int kind, int channels, int bf16, const void* wf, in
  * wrote for the same segments and weights (saved_bytes >=
  * dv_decode_tc_split_save_bytes), out4 its output; the forward is read back,
  * never recomputed.  Adds into grad_voxels and grad_params like dv_decode_bwd.
+ * touched (optional, a byte per grid row): set at each segment's lower corner,
+ * as dv_mark_corner_rows does, so no separate marking launch is needed.
  */
 DV_API int dv_decode_bwd_tc_split(int kind, int channels, const void* wb, int wb_term_bytes,
                                   const int* b_layers, int n_layers, int nvx, int nvy, int nvz,
                                   const float* seg, const int* seg_ray, long long n_seg,
                                   const int64_t* n_seg_dev, const float* pe_feat, const float* d4,
                                   const void* saved, long long saved_bytes, const float* out4,
-                                  float* grad_voxels, float* grad_params, int* err, void* stream);
+                                  float* grad_voxels, float* grad_params, unsigned char* touched, int* err, void* stream);
 
 /* Clearing a grid gradient where a step wrote it (no counterpart in the
  * reference, whose optimizer zeroes the whole dense gradient every step).
