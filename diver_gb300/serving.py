@@ -27,6 +27,8 @@ from dataclasses import dataclass, field
 
 import torch
 
+from .ray_voxel_intersection import PendingSegments
+
 
 @dataclass
 class Request:
@@ -236,7 +238,7 @@ class GpuRenderer:
         for field_model, work, st, o, d, pending in began:
             dev = field_model.voxels.device
             with torch.cuda.stream(st):
-                seg = pending.finish() if hasattr(pending, "finish") else pending
+                seg = pending.finish() if isinstance(pending, PendingSegments) else pending
                 with torch.no_grad():
                     rgb, _ = field_model(o, d, form=self.form, segments=seg)
                 done = []
