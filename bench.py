@@ -84,7 +84,7 @@ def alg_work(kernel, S, U, R):
 # segments, the corner rows and the saved record); the roofline's `traffic`
 # is this times the segments of a launch.  The split backward has no entry:
 # its current form has no ncu section capture (the roofline reports null).
-TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52, "dv_decode_fwd_tc_split": 992.6}
+TRAFFIC_PER_SEG = {"dv_decode_bwd_tc": 1302.35, "dv_decode_fwd_tc": 810.52, "dv_decode_fwd_tc_split": 997.2}
 # Kernels of this library per captured training step: row clear, three weight
 # image gathers, ray PE, slot walk, 3 scan kernels, slot compaction, decoder
 # forward, compositing forward, sparsity mean, loss, loss gradients,
