@@ -222,7 +222,6 @@ __global__ void l2_loss_bwd_kernel(const float* __restrict__ x, const float* __r
 
 using namespace dv;
 
-
 // Decoder kinds: 32 = DIVeR32 (width 32, two hidden layers), 64 = DIVeR64
 // (width 64, one hidden layer); channels 32 or 64.
 static int fill_layers(DecodeArgs& a, int kind, int channels) {

@@ -620,7 +620,6 @@ static int decode_fwd_tc_args(TcArgs& a, int kind, int channels, int terms, cons
   return DV_OK;
 }
 
-
 extern "C" {
 
 int dv_decode_fwd_tc(int kind, int channels, int bf16, const void* wblob, int wbytes, const float* bias, int nbias,

@@ -594,7 +594,8 @@ __global__ void __launch_bounds__(THREADS, 1) decode_bwd_tc_split_kernel(const A
               if (c < IN(l)) atomicAdd(a.grad_params + a.w_off[l] + c * OUT4(l) + o, v[i] + u[i]);
             }
             // layer 3's bias gradient: the PE block's column of ones
-            if (l == 3 && b == 1 && h == 1) atomicAdd(a.grad_params + a.b_off[l] + o, v[PE_ONES - 16] + u[PE_ONES - 16]);
+            if (l == 3 && b == 1 && h == 1)
+              atomicAdd(a.grad_params + a.b_off[l] + o, v[PE_ONES - 16] + u[PE_ONES - 16]);
           }
         }
         if (l != 3 && h == 0) {
